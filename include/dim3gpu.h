@@ -1,0 +1,126 @@
+/*
+ * dim3gpu.h -- C ABI of the GB300 (sm_103a) join-project / join-aggregate
+ * path.  Plain pointers and sizes only.  Every entry point returns a status
+ * code (DIM3G_OK == 0); dim3g_last_error() gives a one-line reason.
+ *
+ * The operation replaces the reference's DIM3 hybrid join-project
+ * (schencoding/JoinProject-DIM3).  Inputs are arrays of interleaved uint32
+ * pairs, the memory layout of the reference's myvector<pair<int,int>>:
+ *   R = (x, y) pairs, S = (z, y) pairs.
+ * The result is the distinct set {(P.first, Q.first) | P.y == Q.y} where P is
+ * the larger input -- R when |R| >= |S|, otherwise S, exactly the reference's
+ * swap (dim3.hpp:993-994), so a smaller R yields (z, x) pairs.  Pairs are
+ * grouped by their first value; the order of groups and of pairs inside a
+ * group is unspecified (the reference's order is unspecified too).
+ *
+ * Limits: |R|, |S| < 2^32 - 1 tuples; the distinct key domains below 2^31;
+ * output counts are 64-bit (no wrap at 2^31, unlike myvector's uint32 count).
+ *
+ * Threading: a context owns one CUDA stream and a workspace; calls on one
+ * context are serialised by the caller, calls on different contexts may run
+ * concurrently.
+ */
+#ifndef DIM3GPU_H
+#define DIM3GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DIM3G_OK 0
+#define DIM3G_ERR_INVALID 1     /* bad argument */
+#define DIM3G_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define DIM3G_ERR_NOMEM 3       /* device or host allocation failed */
+#define DIM3G_ERR_CAPACITY 4    /* output buffer too small; *n_out = pairs needed */
+#define DIM3G_ERR_DEVICE 5      /* a kernel reported a violated bound */
+#define DIM3G_ERR_UNSUPPORTED 6 /* input beyond the supported limits */
+
+typedef struct dim3g_ctx dim3g_ctx;
+
+/* Per-call figures of the last call on a context. */
+typedef struct {
+    uint64_t n_big, n_small;   /* tuples of the larger / smaller input */
+    uint64_t n_small_kept;     /* smaller-input tuples surviving the semi-join */
+    uint64_t out_j;            /* exact join size sum_b degP(b) * degQ(b) */
+    uint64_t n_out;            /* distinct output pairs (groups) */
+    uint32_t swapped;          /* 1 when |R| < |S| */
+    uint32_t nx, ny, nz;       /* distinct first / join / second values */
+    uint32_t rows_warp, rows_block, rows_bitmap, rows_dense; /* x rows per kernel class */
+    uint32_t z_tiles;          /* z tiles of the bitmap class */
+    uint32_t heavy_y;          /* join values whose S rows went to the dense block */
+    float ms_map;              /* device ms: hash build, probe, id assignment */
+    float ms_csr;              /* device ms: CSR builds, row binning */
+    float ms_count;            /* device ms: count pass + offsets */
+    float ms_write;            /* device ms: write pass */
+    float ms_total;            /* device ms: whole call (inputs resident) */
+} dim3g_stats;
+
+/* ---- context ------------------------------------------------------- */
+int dim3g_create(int device, dim3g_ctx** ctx);
+void dim3g_destroy(dim3g_ctx* ctx);
+/* Use the caller's cudaStream_t for all work of this context (NULL restores
+ * the context's own stream). */
+int dim3g_set_stream(dim3g_ctx* ctx, void* cuda_stream);
+const char* dim3g_last_error(const dim3g_ctx* ctx);
+int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
+/* Tuning knobs, validated on set: "warp_slots_log2" (5..11, warp-class hash
+ * set size), "block_slots_log2" (8..14, block-class hash set size),
+ * "tile_bits_log2" (10..20, bitmap-class z tile width), "heavy_min_len"
+ * (minimum S row length for the dense bitmap block; 0 disables it). */
+int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
+int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
+/* Release device memory cached by the context (workspace, staging). */
+int dim3g_trim(dim3g_ctx* ctx);
+
+/* ---- join-project --------------------------------------------------
+ * Replaces DIM3<int,int,int,...>::doJoinProject (dim3.hpp:982-1055) and
+ * DIM3_parallel<...>::doJoinProject_parallel (dim3_parallel.hpp:137-210):
+ * the same R, S and result, with the result as interleaved pairs. */
+
+/* Host input, result in a malloc'd host array (free with free()); this is the
+ * ownership of the reference's myvector result (malloc/realloc'd data). */
+int dim3g_join_project(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy,
+                       uint64_t nS, uint32_t** out_xz, uint64_t* n_out);
+/* Host input, result into the caller's host buffer of `capacity` pairs
+ * (pinned memory gives full copy bandwidth). */
+int dim3g_join_project_into(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy,
+                            uint64_t nS, uint32_t* out_xz, uint64_t capacity, uint64_t* n_out);
+/* Device-resident input and output: d_R, d_S, d_out are device pointers
+ * (8-byte aligned).  On DIM3G_ERR_CAPACITY nothing is written and *n_out
+ * holds the pairs needed. */
+int dim3g_join_project_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S,
+                              uint64_t nS, uint32_t* d_out, uint64_t capacity, uint64_t* n_out);
+/* Count only: the number of distinct pairs, no pairs written. */
+int dim3g_join_project_count_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S,
+                                    uint64_t nS, uint64_t* n_out);
+
+/* ---- join-aggregate COUNT(*) GROUP BY (x, z) -------------------------
+ * Replaces DIM3JoinAggregate<...>::doJoinAggregate (dim3.hpp:1313-1373) with
+ * a COUNT aggregate: for every distinct (P.first, Q.first) the number of
+ * joining tuple pairs, exact in 64 bits. */
+int dim3g_join_count(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy, uint64_t nS,
+                     uint32_t** out_xz, uint64_t** out_cnt, uint64_t* n_out);
+int dim3g_join_count_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
+                            uint32_t* d_out_xz, uint64_t* d_out_cnt, uint64_t capacity, uint64_t* n_out);
+
+/* ---- L+S mapper -----------------------------------------------------
+ * Replaces LS_mapper<T,H,Tcounter> (Include/L+S_mapper.hpp:11-160): a GPU
+ * value -> dense id map.  insert() gives every key its existing id or the
+ * next dense id, in the order of first occurrence inside the batch, exactly
+ * as a sequence of the reference's insert() calls would; find() gives the id
+ * or -1.  Keys are any 32-bit values; ids are int32. */
+typedef struct dim3g_mapper dim3g_mapper;
+int dim3g_mapper_create(dim3g_ctx* ctx, uint64_t capacity_hint, dim3g_mapper** m);
+void dim3g_mapper_destroy(dim3g_mapper* m);
+int dim3g_mapper_insert(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32_t* ids_out);
+int dim3g_mapper_find(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32_t* ids_out);
+int64_t dim3g_mapper_size(const dim3g_mapper* m);
+/* clear(): drop all keys, keep the id counter (L+S_mapper.hpp:37-40). */
+int dim3g_mapper_clear(dim3g_mapper* m);
+/* reset_cnt() / __set_cnt(v) (L+S_mapper.hpp:42-48). */
+int dim3g_mapper_set_cnt(dim3g_mapper* m, int64_t cnt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

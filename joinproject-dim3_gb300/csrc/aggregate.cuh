@@ -1,0 +1,187 @@
+// aggregate.cuh -- COUNT(*) GROUP BY (x, z): the write pass of the
+// join-aggregate (SpmmAggregate with a COUNT plug-in, dim3.hpp:1271-1310).
+//
+// The count pass is the join-project count pass (distinct z per row).  The
+// write pass expands each row again with a per-z counter -- a shared-memory
+// hash map (z -> count) for classes 1 and 2, a shared-memory counter array
+// over one z tile for class 3 -- and then emits every (x, z, count) of the
+// row at off[x] + a row-local slot.  Counts are exact: each expansion
+// candidate is one joining (R tuple, S tuple) pair.
+#pragma once
+#include "common.cuh"
+#include "expand.cuh"
+
+namespace dim3g {
+
+struct AggOut {
+    unsigned long long* cnt;  // one count per output pair
+};
+
+// Shared-memory map slot of z (inserting it if absent).
+__device__ __forceinline__ uint32_t smem_map_slot(uint32_t* keys, uint32_t lg, uint32_t z, uint32_t* err) {
+    const uint32_t mask = (1u << lg) - 1;
+    uint32_t h = (z * 0x9E3779B1u) >> (32 - lg);
+    volatile uint32_t* vk = keys;
+    for (uint32_t p = 0; p <= mask; p++) {
+        uint32_t cur = vk[h];
+        if (cur == z) return h;
+        if (cur == kEmpty32) {
+            uint32_t prev = atomicCAS(&keys[h], kEmpty32, z);
+            if (prev == kEmpty32 || prev == z) return h;
+        }
+        h = (h + 1) & mask;
+    }
+    raise_error(err, kErrTableFull);
+    return 0xFFFFFFFFu;
+}
+
+// Warp-collective emission of occupied map slots [s0, s1) with stride 32.
+// *pos is the row-local running slot (warp-uniform for class 1; for class 2
+// the caller passes a shared counter through `shared_pos`).
+__device__ __forceinline__ void emit_map_slots_warp(const RowCtx& c, AggOut ao, const uint32_t* keys,
+                                                    const uint32_t* vals, uint32_t s0, uint32_t s1, uint32_t xv,
+                                                    unsigned long long base, uint32_t lim, uint32_t* shared_pos,
+                                                    uint32_t* local_pos) {
+    const uint32_t lane = lane_id();
+    for (uint32_t sb = s0; sb < s1; sb += 32) {
+        uint32_t s = sb + lane;
+        uint32_t key = (s < s1) ? keys[s] : kEmpty32;
+        bool occ = key != kEmpty32;
+        uint32_t b = __ballot_sync(0xffffffffu, occ);
+        if (!b) continue;
+        uint32_t pb;
+        if (shared_pos) {
+            pb = 0;
+            if (lane == 0) pb = atomicAdd(shared_pos, (uint32_t)__popc(b));
+            pb = __shfl_sync(0xffffffffu, pb, 0);
+        } else {
+            pb = *local_pos;
+            *local_pos += __popc(b);
+        }
+        if (occ) {
+            uint32_t pos = pb + __popc(b & lanemask_lt());
+            if (pos < lim) {
+                c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[key]));
+                ao.cnt[base + pos] = vals[s];
+            } else {
+                raise_error(c.err, kErrOutputBound);
+            }
+        }
+    }
+}
+
+// Class 1 write pass: one warp per row; per warp 2^lg keys + 2^lg counts.
+__global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+                                                  const uint32_t* __restrict__ nrows_p, uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    uint32_t* keys = smem + ((size_t)wib << (warp_lg + 1));
+    uint32_t* vals = keys + (1u << warp_lg);
+    const uint32_t nrows = *nrows_p;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
+        const uint32_t x = rows[ri];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
+        for (uint32_t s = lane; s < (1u << lg); s += 32) {
+            keys[s] = kEmpty32;
+            vals[s] = 0;
+        }
+        __syncwarp();
+        auto ins = [&](uint32_t z) {
+            uint32_t s = smem_map_slot(keys, lg, z, c.err);
+            if (s != 0xFFFFFFFFu) atomicAdd(&vals[s], 1u);
+            return false;
+        };
+        auto emit = [&](bool, uint32_t) {};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 32, 0, c.T, ins, emit);
+        __syncwarp();
+        uint32_t pos = 0;
+        emit_map_slots_warp(c, ao, keys, vals, 0, 1u << lg, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+        __syncwarp();
+    }
+}
+
+// Class 2 write pass: one CTA per row.
+__global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+                                                   const uint32_t* __restrict__ nrows_p, uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_pos;
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5;
+    uint32_t* keys = smem;
+    uint32_t* vals = smem + (1u << block_lg);
+    const uint32_t nrows = *nrows_p;
+    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const uint32_t x = rows[ri];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+        for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
+            keys[s] = kEmpty32;
+            vals[s] = 0;
+        }
+        if (threadIdx.x == 0) s_pos = 0;
+        __syncthreads();
+        auto ins = [&](uint32_t z) {
+            uint32_t s = smem_map_slot(keys, lg, z, c.err);
+            if (s != 0xFFFFFFFFu) atomicAdd(&vals[s], 1u);
+            return false;
+        };
+        auto emit = [&](bool, uint32_t) {};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, 0, c.T, ins, emit);
+        __syncthreads();
+        const uint32_t span = (1u << lg);
+        const uint32_t per = (span + nw - 1) / nw;
+        const uint32_t s0 = min(span, wib * per), s1 = min(span, s0 + per);
+        emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        __syncthreads();
+    }
+}
+
+// Class 3 write pass: one CTA per row; a counter per z of one tile.
+__global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+                                                   const uint32_t* __restrict__ nrows_p) {
+    extern __shared__ uint32_t ctr[];
+    __shared__ uint32_t s_pos;
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t nrows = *nrows_p;
+    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const uint32_t x = rows[ri];
+        const unsigned long long base = c.off[x];
+        const uint32_t lim = c.cnt[x], xv = c.id2x[x];
+        if (threadIdx.x == 0) s_pos = 0;
+        for (uint32_t t = 0; t < c.T; t++) {
+            const uint32_t lo = t * c.tile_width;
+            const uint32_t width = min(c.tile_width, c.m - lo);
+            for (uint32_t w = threadIdx.x; w < width; w += blockDim.x) ctr[w] = 0;
+            __syncthreads();
+            auto ins = [&](uint32_t z) {
+                atomicAdd(&ctr[z - lo], 1u);
+                return false;
+            };
+            auto emit = [&](bool, uint32_t) {};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, t, t + 1, ins, emit);
+            __syncthreads();
+            // emit the nonzero counters of this tile
+            for (uint32_t wb = wib * 32; wb < width; wb += nw * 32) {
+                uint32_t w = wb + lane;
+                uint32_t v = w < width ? ctr[w] : 0;
+                uint32_t b = __ballot_sync(0xffffffffu, v != 0);
+                if (!b) continue;
+                uint32_t pb = 0;
+                if (lane == 0) pb = atomicAdd(&s_pos, (uint32_t)__popc(b));
+                pb = __shfl_sync(0xffffffffu, pb, 0);
+                if (v) {
+                    uint32_t pos = pb + __popc(b & lanemask_lt());
+                    if (pos < lim) {
+                        c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[lo + w]));
+                        ao.cnt[base + pos] = v;
+                    } else {
+                        raise_error(c.err, kErrOutputBound);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace dim3g

@@ -1,0 +1,80 @@
+// common.cuh -- shared device helpers for the DIM3 GB300 join-project path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dim3g {
+
+constexpr int kWarp = 32;
+constexpr uint64_t kEmpty64 = ~0ull;
+
+// Error flags written by kernels into a device word; the host reads it after
+// each call and turns any set bit into a status code.
+enum DeviceError : uint32_t {
+    kErrProbeLimit = 1u,    // an open-addressing probe ran past the table size
+    kErrTableFull = 2u,     // a shared-memory table overflowed its sizing bound
+    kErrOutputBound = 4u,   // a write-pass position ran past the row's count
+    kErrCountRange = 8u,    // a per-group count could exceed 32 bits
+};
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
+
+// murmur3 fmix32: the GPU tables use their own mixing hash (the reference's
+// identity hash clusters adjacent keys under linear probing).
+__device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Inclusive warp scan.
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T t = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane_id() >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive block scan of one value per thread; returns the prefix and the
+// block total through *total.  smem must hold BLOCK/32 + 1 T.
+template <int BLOCK, typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* smem, T* total) {
+    constexpr int NW = BLOCK / 32;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    T inc = warp_incl_scan(v);
+    if (l == 31) smem[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        T s = (l < NW) ? smem[l] : T(0);
+        T si = warp_incl_scan(s);
+        if (l < NW) smem[l] = si - s;
+        if (l == NW - 1) smem[NW] = si;
+    }
+    __syncthreads();
+    T r = smem[w] + inc - v;
+    *total = smem[NW];
+    __syncthreads();
+    return r;
+}
+
+}  // namespace dim3g

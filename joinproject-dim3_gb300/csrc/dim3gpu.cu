@@ -1,0 +1,822 @@
+// dim3gpu.cu -- host orchestration and C ABI of the GB300 join-project path.
+//
+// One call runs, on the context's stream:
+//   mapping   hash build on P (first column, y), semi-join probe of Q with z
+//             insertion, dense ids by prefix sums over occupied slots
+//             (replaces mapping_step + LS_mapper, dim3.hpp:394-883)
+//   CSR       R by x id, S by (y id, z tile) (divide_R / divide_S,
+//             dim3.hpp:1058-1259), per-row work and row binning
+//   count     per-row distinct counts, prefix sum to output offsets
+//   write     the same expansion emitting (x value, z value) pairs
+// (Hybrid_solution, dim3.hpp:889-974).  Two host synchronisations: one for
+// the id domain sizes, one for the output size.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/dim3gpu.h"
+#include "aggregate.cuh"
+#include "common.cuh"
+#include "expand.cuh"
+#include "mapper.cuh"
+#include "mapping.cuh"
+#include "scan.cuh"
+
+using namespace dim3g;
+
+namespace {
+
+// ------------------------------------------------------------ workspace
+// Grow-only list of device blocks with a bump pointer each; reset at the
+// start of every call, so repeated calls of the same shape reuse the same
+// addresses and never allocate.
+struct Arena {
+    struct Block {
+        char* p;
+        size_t size, used;
+    };
+    std::vector<Block> blocks;
+    void reset() {
+        for (auto& b : blocks) b.used = 0;
+    }
+    void* alloc(size_t bytes) {
+        bytes = (bytes + 255) & ~(size_t)255;
+        if (bytes == 0) bytes = 256;
+        for (auto& b : blocks)
+            if (b.size - b.used >= bytes) {
+                void* r = b.p + b.used;
+                b.used += bytes;
+                return r;
+            }
+        size_t sz = bytes < ((size_t)256 << 20) ? ((size_t)256 << 20) : bytes;
+        char* p = nullptr;
+        if (cudaMalloc(&p, sz) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        blocks.push_back({p, sz, bytes});
+        return p;
+    }
+    void release() {
+        for (auto& b : blocks) cudaFree(b.p);
+        blocks.clear();
+    }
+};
+
+struct Params {
+    uint32_t warp_lg = 11;    // 2048 slots per warp set  -> class 1 up to 1024
+    uint32_t block_lg = 14;   // 16384 slots per CTA set  -> class 2 up to 8192
+    uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
+    int64_t heavy_min_len = 0;
+};
+
+constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
+
+struct Scalars {
+    unsigned long long nx, ny, nz, nkept, total, outj;
+    unsigned long long nrows[4];
+    unsigned int err;
+    unsigned int pad;
+};
+
+}  // namespace
+
+struct dim3g_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    Arena ws;
+    Params prm;
+    dim3g_stats stats{};
+    // host-API staging (device) buffers, grow-only
+    void* d_in = nullptr;
+    size_t d_in_bytes = 0;
+    void* d_out = nullptr;
+    size_t d_out_bytes = 0;
+    Scalars* h_sc = nullptr;  // pinned
+    cudaEvent_t ev[6] = {};
+};
+
+struct dim3g_mapper {
+    dim3g_ctx* ctx;
+    unsigned long long* slots = nullptr;
+    uint64_t cap = 0;
+    int64_t cnt = 0;
+    int64_t nkeys = 0;
+};
+
+namespace {
+
+int fail(dim3g_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(c, DIM3G_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CHECK_LAUNCH() CU(cudaGetLastError())
+
+uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+unsigned grid_for(uint64_t n, int sm, int per_sm = 8, int block = 256) {
+    uint64_t b = (n + block - 1) / block;
+    uint64_t cap = (uint64_t)sm * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+template <class T>
+T* ws_get(dim3g_ctx* c, uint64_t count) {
+    return (T*)c->ws.alloc(count * sizeof(T));
+}
+
+// Where the write pass puts its result: called once the count pass knows the
+// number of output pairs; returns the device buffers or an error status.
+struct OutPrep {
+    int (*fn)(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned long long** cnt);
+    void* user;
+};
+
+// Device state of one join call.
+struct JoinPlan {
+    const uint2* P;
+    uint64_t nP;
+    const uint2* Q;
+    uint64_t nQ;
+    bool swapped;
+    bool aggregate;   // COUNT(*) per group instead of distinct pairs
+    bool count_only;  // stop after the count pass
+    OutPrep prep;
+};
+
+bool set_aggregate_attributes();
+int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const uint32_t* list_w, const uint32_t* list_b,
+                        const uint32_t* list_m, const uint32_t* nr_w, const uint32_t* nr_b, const uint32_t* nr_m);
+
+int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
+    cudaStream_t st = c->stream;
+    c->ws.reset();
+    dim3g_stats& S = c->stats;
+    memset(&S, 0, sizeof S);
+    S.n_big = jp.nP;
+    S.n_small = jp.nQ;
+    S.swapped = jp.swapped;
+    *n_out = 0;
+    if (jp.nP >= 0xFFFFFFFFull || jp.nQ >= 0xFFFFFFFFull)
+        return fail(c, DIM3G_ERR_UNSUPPORTED, "relations of 2^32-1 or more tuples are not supported");
+    if (jp.nP == 0 || jp.nQ == 0) return DIM3G_OK;
+    const int sm = c->sm_count;
+    CU(cudaEventRecord(c->ev[0], st));
+
+    Scalars* sc = ws_get<Scalars>(c, 1);
+    const uint64_t capP = next_pow2(jp.nP * 2 < 1024 ? 1024 : jp.nP * 2);
+    const uint64_t capQ = next_pow2(jp.nQ * 2 < 1024 ? 1024 : jp.nQ * 2);
+    DevTable tx{ws_get<unsigned long long>(c, capP), capP - 1};
+    DevTable ty{ws_get<unsigned long long>(c, capP), capP - 1};
+    DevTable tz{ws_get<unsigned long long>(c, capQ), capQ - 1};
+    uint2* Qk = ws_get<uint2>(c, jp.nQ);
+    uint2* Pm = ws_get<uint2>(c, jp.nP);
+    uint32_t* id2x = ws_get<uint32_t>(c, jp.nP);
+    uint32_t* id2z = ws_get<uint32_t>(c, jp.nQ);
+    uint64_t* bsum = ws_get<uint64_t>(c, scan_blocks(capP > capQ ? capP : capQ) + 1);
+    if (!sc || !tx.slots || !ty.slots || !tz.slots || !Qk || !Pm || !id2x || !id2z || !bsum)
+        return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
+
+    CU(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
+    CU(cudaMemsetAsync(tx.slots, 0xff, capP * 8, st));
+    CU(cudaMemsetAsync(ty.slots, 0xff, capP * 8, st));
+    CU(cudaMemsetAsync(tz.slots, 0xff, capQ * 8, st));
+
+    k_insert_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, &sc->err);
+    CHECK_LAUNCH();
+    device_scan(OccupiedSrc{ty.slots}, AssignIdDst{ty.slots, nullptr}, capP, bsum, &sc->ny, st);
+    device_scan(OccupiedSrc{tx.slots}, AssignIdDst{tx.slots, id2x}, capP, bsum, &sc->nx, st);
+    k_probe_q<<<grid_for(jp.nQ, sm), 256, 0, st>>>(jp.Q, jp.nQ, ty, tz, Qk, &sc->nkept, &sc->err);
+    CHECK_LAUNCH();
+    device_scan(OccupiedSrc{tz.slots}, AssignIdDst{tz.slots, id2z}, capQ, bsum, &sc->nz, st);
+    CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in mapping (flags %u)", c->h_sc->err);
+    const uint32_t n = (uint32_t)c->h_sc->nx, k = (uint32_t)c->h_sc->ny, m = (uint32_t)c->h_sc->nz;
+    const uint64_t nq = c->h_sc->nkept;
+    S.nx = n;
+    S.ny = k;
+    S.nz = m;
+    S.n_small_kept = nq;
+    CU(cudaEventRecord(c->ev[1], st));
+    if (nq == 0) {
+        S.ms_total = 0;
+        return DIM3G_OK;
+    }
+    if (m >= 0x80000000u || n >= 0x80000000u)
+        return fail(c, DIM3G_ERR_UNSUPPORTED, "key domains of 2^31 or more distinct values are not supported");
+
+    // z tiles for the bitmap class
+    uint32_t tile_lg = jp.aggregate ? kAggTileLg : c->prm.tile_lg;
+    uint32_t T = 1, tile_shift = 31, tile_width = m;
+    if (m > (1u << tile_lg)) {
+        tile_shift = tile_lg;
+        tile_width = 1u << tile_lg;
+        T = (m + tile_width - 1) >> tile_lg;
+    }
+    if ((uint64_t)k * T >= 0xFFFFFFFFull)
+        return fail(c, DIM3G_ERR_UNSUPPORTED, "join domain x z tiles too large");
+    S.z_tiles = T;
+    const uint64_t nyt = (uint64_t)k * T;
+
+    uint32_t* degx = ws_get<uint32_t>(c, (uint64_t)n + 1);
+    uint32_t* curx = ws_get<uint32_t>(c, (uint64_t)n + 1);
+    uint32_t* JR_R = ws_get<uint32_t>(c, (uint64_t)n + 1);
+    uint32_t* IC_R = ws_get<uint32_t>(c, jp.nP);
+    uint32_t* cnt_yt = ws_get<uint32_t>(c, nyt + 1);
+    uint32_t* cur_yt = ws_get<uint32_t>(c, nyt + 1);
+    uint32_t* JR_S = ws_get<uint32_t>(c, nyt + 1);
+    uint32_t* IC_S = ws_get<uint32_t>(c, nq);
+    uint32_t* ucap = ws_get<uint32_t>(c, n);
+    uint8_t* cls = ws_get<uint8_t>(c, n);
+    uint32_t* lists = ws_get<uint32_t>(c, (uint64_t)3 * n);
+    uint32_t* cnt = ws_get<uint32_t>(c, n);
+    unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
+    uint64_t* bsum2 = ws_get<uint64_t>(c, scan_blocks((nyt > n ? nyt : n) + 1) + 1);
+    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !ucap || !cls || !lists ||
+        !cnt || !off || !bsum2)
+        return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
+
+    CU(cudaMemsetAsync(degx, 0, ((uint64_t)n + 1) * 4, st));
+    CU(cudaMemsetAsync(cnt_yt, 0, (nyt + 1) * 4, st));
+    k_map_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, Pm, degx);
+    CHECK_LAUNCH();
+    k_map_q<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, tz, T, tile_shift, cnt_yt);
+    CHECK_LAUNCH();
+    device_scan(U32Src{degx}, RowPtrDst{JR_R, curx}, (uint64_t)n + 1, bsum2, nullptr, st);
+    k_scatter_r<<<grid_for(jp.nP, sm), 256, 0, st>>>(Pm, jp.nP, curx, IC_R);
+    CHECK_LAUNCH();
+    device_scan(U32Src{cnt_yt}, RowPtrDst{JR_S, cur_yt}, nyt + 1, bsum2, nullptr, st);
+    k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, T, tile_shift, cur_yt, IC_S);
+    CHECK_LAUNCH();
+
+    RowCtx rc{};
+    rc.JR_R = JR_R;
+    rc.IC_R = IC_R;
+    rc.JR_S = JR_S;
+    rc.IC_S = IC_S;
+    rc.T = T;
+    rc.tile_width = tile_width;
+    rc.m = m;
+    rc.ucap = ucap;
+    rc.cnt = cnt;
+    rc.off = off;
+    rc.id2x = id2x;
+    rc.id2z = id2z;
+    rc.out = nullptr;
+    rc.err = &sc->err;
+    const uint32_t cap_w = 1u << (c->prm.warp_lg - 1);
+    const uint32_t cap_b = 1u << (c->prm.block_lg - 1);
+    k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, ucap, cls,
+                                                                &sc->outj);
+    CHECK_LAUNCH();
+    uint32_t* list_w = lists;
+    uint32_t* list_b = lists + n;
+    uint32_t* list_m = lists + 2 * (uint64_t)n;
+    device_scan(ClassSrc{cls, 1}, ListDst{list_w}, n, bsum2, &sc->nrows[1], st);
+    device_scan(ClassSrc{cls, 2}, ListDst{list_b}, n, bsum2, &sc->nrows[2], st);
+    device_scan(ClassSrc{cls, 3}, ListDst{list_m}, n, bsum2, &sc->nrows[3], st);
+    CU(cudaMemsetAsync(cnt, 0, (uint64_t)n * 4, st));
+    CU(cudaEventRecord(c->ev[2], st));
+
+    // nrows are read on the device; the grids are fixed multiples of the SMs
+    const uint32_t* nr_w = (const uint32_t*)&sc->nrows[1];
+    const uint32_t* nr_b = (const uint32_t*)&sc->nrows[2];
+    const uint32_t* nr_m = (const uint32_t*)&sc->nrows[3];
+    const size_t smem_w = (size_t)8 << c->prm.warp_lg << 2;
+    const size_t smem_b = (size_t)1 << c->prm.block_lg << 2;
+    const size_t smem_m = (size_t)((tile_width + 31) / 32) * 4;
+    const unsigned g_w = (unsigned)sm * 4, g_b = (unsigned)sm * 3, g_m = (unsigned)sm * 2;
+
+    k_rows_warp<false><<<g_w, 256, smem_w, st>>>(rc, list_w, nr_w, c->prm.warp_lg);
+    CHECK_LAUNCH();
+    k_rows_block<false><<<g_b, 256, smem_b, st>>>(rc, list_b, nr_b, c->prm.block_lg);
+    CHECK_LAUNCH();
+    k_rows_bitmap<false><<<g_m, 512, smem_m, st>>>(rc, list_m, nr_m);
+    CHECK_LAUNCH();
+    device_scan(U32Src{cnt}, OffDst{off}, (uint64_t)n + 1, bsum2, &sc->total, st);
+    CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    CU(cudaEventRecord(c->ev[3], st));
+    CU(cudaStreamSynchronize(st));
+    if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in count pass (flags %u)", c->h_sc->err);
+    const uint64_t total = c->h_sc->total;
+    S.out_j = c->h_sc->outj;
+    S.n_out = total;
+    S.rows_warp = (uint32_t)c->h_sc->nrows[1];
+    S.rows_block = (uint32_t)c->h_sc->nrows[2];
+    S.rows_bitmap = (uint32_t)c->h_sc->nrows[3];
+    *n_out = total;
+    if (jp.count_only) {
+        float a, b, d;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&d, c->ev[2], c->ev[3]);
+        S.ms_map = a;
+        S.ms_csr = b;
+        S.ms_count = d;
+        S.ms_total = a + b + d;
+        return DIM3G_OK;
+    }
+    uint2* out = nullptr;
+    unsigned long long* out_cnt = nullptr;
+    int pr = jp.prep.fn(c, jp.prep.user, total, &out, &out_cnt);
+    if (pr) return pr;
+    rc.out = out;
+    if (total > 0) {
+        if (jp.aggregate) {
+            int r = run_aggregate_write(c, rc, AggOut{out_cnt}, list_w, list_b, list_m, nr_w, nr_b, nr_m);
+            if (r) return r;
+        } else {
+            k_rows_warp<true><<<g_w, 256, smem_w, st>>>(rc, list_w, nr_w, c->prm.warp_lg);
+            CHECK_LAUNCH();
+            k_rows_block<true><<<g_b, 256, smem_b, st>>>(rc, list_b, nr_b, c->prm.block_lg);
+            CHECK_LAUNCH();
+            k_rows_bitmap<true><<<g_m, 512, smem_m, st>>>(rc, list_m, nr_m);
+            CHECK_LAUNCH();
+        }
+    }
+    CU(cudaMemcpyAsync(&c->h_sc->err, &sc->err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    CU(cudaEventRecord(c->ev[4], st));
+    CU(cudaStreamSynchronize(st));
+    if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in write pass (flags %u)", c->h_sc->err);
+    float a, b, d, e;
+    cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&d, c->ev[2], c->ev[3]);
+    cudaEventElapsedTime(&e, c->ev[3], c->ev[4]);
+    S.ms_map = a;
+    S.ms_csr = b;
+    S.ms_count = d;
+    S.ms_write = e;
+    S.ms_total = a + b + d + e;
+    return DIM3G_OK;
+}
+
+int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const uint32_t* list_w, const uint32_t* list_b,
+                        const uint32_t* list_m, const uint32_t* nr_w, const uint32_t* nr_b, const uint32_t* nr_m) {
+    cudaStream_t st = c->stream;
+    const int sm = c->sm_count;
+    const size_t smem_w = (size_t)8 << (c->prm.warp_lg + 1) << 2;
+    const size_t smem_b = (size_t)2 << c->prm.block_lg << 2;
+    const size_t smem_m = (size_t)rc.tile_width * 4;
+    k_agg_warp<<<(unsigned)sm * 2, 256, smem_w, st>>>(rc, ao, list_w, nr_w, c->prm.warp_lg);
+    CHECK_LAUNCH();
+    k_agg_block<<<(unsigned)sm * 2, 256, smem_b, st>>>(rc, ao, list_b, nr_b, c->prm.block_lg);
+    CHECK_LAUNCH();
+    k_agg_tile<<<(unsigned)sm, 1024, smem_m, st>>>(rc, ao, list_m, nr_m);
+    CHECK_LAUNCH();
+    return DIM3G_OK;
+}
+
+bool set_aggregate_attributes() {
+    return cudaFuncSetAttribute(k_agg_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 12 << 2) == cudaSuccess &&
+           cudaFuncSetAttribute(k_agg_block, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 << 14 << 2) == cudaSuccess &&
+           cudaFuncSetAttribute(k_agg_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (1 << kAggTileLg) * 4) == cudaSuccess;
+}
+
+int ensure_dev(dim3g_ctx* c, void** p, size_t* have, size_t need) {
+    if (*have >= need && *p) return DIM3G_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    size_t sz = need < 4096 ? 4096 : need;
+    if (cudaMalloc(p, sz) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(c, DIM3G_ERR_NOMEM, "device allocation of %zu bytes failed", sz);
+    }
+    *have = sz;
+    return DIM3G_OK;
+}
+
+bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+
+// Output preparation for device-resident callers: their buffer and capacity.
+struct DeviceOut {
+    uint2* out;
+    unsigned long long* cnt;
+    uint64_t capacity;
+};
+int prep_device(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned long long** cnt) {
+    DeviceOut* d = (DeviceOut*)user;
+    if (total > d->capacity)
+        return fail(c, DIM3G_ERR_CAPACITY, "output needs %llu pairs, capacity is %llu", (unsigned long long)total,
+                    (unsigned long long)d->capacity);
+    *out = d->out;
+    *cnt = d->cnt;
+    return DIM3G_OK;
+}
+
+// Output preparation for host callers: the context's grow-only device staging.
+struct StagingOut {
+    bool aggregate;
+};
+int prep_staging(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned long long** cnt) {
+    bool agg = ((StagingOut*)user)->aggregate;
+    int r = ensure_dev(c, &c->d_out, &c->d_out_bytes, total * (agg ? 16 : 8));
+    if (r) return r;
+    *out = (uint2*)c->d_out;
+    *cnt = agg ? (unsigned long long*)((char*)c->d_out + total * 8) : nullptr;
+    return DIM3G_OK;
+}
+
+// Host-input join: stage R and S on the device, run, copy the result back
+// into the caller's buffer (out_into) or a malloc'd one (out_alloc).
+int host_join(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, uint64_t nS, bool aggregate,
+              uint32_t** out_alloc, uint64_t** cnt_alloc, uint32_t* out_into, uint64_t capacity, uint64_t* n_out) {
+    if (!c) return DIM3G_ERR_INVALID;
+    if (!n_out || (nR && !R) || (nS && !S)) return fail(c, DIM3G_ERR_INVALID, "null argument");
+    *n_out = 0;
+    if (out_alloc) *out_alloc = nullptr;
+    if (cnt_alloc) *cnt_alloc = nullptr;
+    CU(cudaSetDevice(c->device));
+    const bool swap = nR < nS;
+    const uint32_t* P = swap ? S : R;
+    const uint32_t* Q = swap ? R : S;
+    const uint64_t nP = swap ? nS : nR, nQ = swap ? nR : nS;
+    int r = ensure_dev(c, &c->d_in, &c->d_in_bytes, (nP + nQ) * 8 + 256);
+    if (r) return r;
+    uint2* dP = (uint2*)c->d_in;
+    uint2* dQ = dP + nP;
+    cudaStream_t st = c->stream;
+    if (nP) CU(cudaMemcpyAsync(dP, P, nP * 8, cudaMemcpyHostToDevice, st));
+    if (nQ) CU(cudaMemcpyAsync(dQ, Q, nQ * 8, cudaMemcpyHostToDevice, st));
+    StagingOut so{aggregate};
+    JoinPlan jp{dP, nP, dQ, nQ, swap, aggregate, false, OutPrep{prep_staging, &so}};
+    uint64_t n = 0;
+    r = run_join(c, jp, &n);
+    if (r) return r;
+    *n_out = n;
+    const uint2* dout = (const uint2*)c->d_out;
+    const unsigned long long* dcnt = aggregate ? (const unsigned long long*)((const char*)c->d_out + n * 8) : nullptr;
+    if (out_into) {
+        if (n > capacity)
+            return fail(c, DIM3G_ERR_CAPACITY, "output needs %llu pairs, capacity is %llu", (unsigned long long)n,
+                        (unsigned long long)capacity);
+        if (n) CU(cudaMemcpyAsync(out_into, dout, n * 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        return DIM3G_OK;
+    }
+    uint32_t* h = (uint32_t*)malloc(n ? n * 8 : 8);
+    uint64_t* hc = nullptr;
+    if (!h) return fail(c, DIM3G_ERR_NOMEM, "host allocation of %llu pairs failed", (unsigned long long)n);
+    if (aggregate) {
+        hc = (uint64_t*)malloc(n ? n * 8 : 8);
+        if (!hc) {
+            free(h);
+            return fail(c, DIM3G_ERR_NOMEM, "host allocation of %llu counts failed", (unsigned long long)n);
+        }
+    }
+    if (n) {
+        cudaError_t e1 = cudaMemcpyAsync(h, dout, n * 8, cudaMemcpyDeviceToHost, st);
+        cudaError_t e2 = aggregate ? cudaMemcpyAsync(hc, dcnt, n * 8, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+        cudaError_t e3 = cudaStreamSynchronize(st);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+            free(h);
+            free(hc);
+            return fail(c, DIM3G_ERR_CUDA, "result copy failed: %s",
+                        cudaGetErrorString(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3)));
+        }
+    }
+    *out_alloc = h;
+    if (cnt_alloc) *cnt_alloc = hc;
+    return DIM3G_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int dim3g_create(int device, dim3g_ctx** out) {
+    if (!out) return DIM3G_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return DIM3G_ERR_CUDA;
+    }
+    dim3g_ctx* c = new dim3g_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaMallocHost((void**)&c->h_sc, sizeof(Scalars)) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return DIM3G_ERR_CUDA;
+    }
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    c->stream = c->own_stream;
+    // Shared-memory carve-outs for the expansion kernels (largest settings).
+    const int smem_w = 8 << 11 << 2, smem_b = 1 << 14 << 2, smem_m = (1 << 20) / 8;
+    bool ok = cudaFuncSetAttribute(k_rows_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_w) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_w) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_bitmap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_bitmap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
+              set_aggregate_attributes();
+    if (!ok) {
+        cudaGetLastError();
+        dim3g_destroy(c);
+        return DIM3G_ERR_CUDA;
+    }
+    *out = c;
+    return DIM3G_OK;
+}
+
+void dim3g_destroy(dim3g_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->ws.release();
+    if (c->d_in) cudaFree(c->d_in);
+    if (c->d_out) cudaFree(c->d_out);
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+int dim3g_set_stream(dim3g_ctx* c, void* s) {
+    if (!c) return DIM3G_ERR_INVALID;
+    c->stream = s ? (cudaStream_t)s : c->own_stream;
+    return DIM3G_OK;
+}
+
+const char* dim3g_last_error(const dim3g_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int dim3g_get_stats(const dim3g_ctx* c, dim3g_stats* out) {
+    if (!c || !out) return DIM3G_ERR_INVALID;
+    *out = c->stats;
+    return DIM3G_OK;
+}
+
+int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
+    if (!c || !name) return DIM3G_ERR_INVALID;
+    if (!strcmp(name, "warp_slots_log2")) {
+        if (v < 5 || v > 11) return fail(c, DIM3G_ERR_INVALID, "warp_slots_log2 must be in 5..11");
+        c->prm.warp_lg = (uint32_t)v;
+    } else if (!strcmp(name, "block_slots_log2")) {
+        if (v < 8 || v > 14) return fail(c, DIM3G_ERR_INVALID, "block_slots_log2 must be in 8..14");
+        if ((uint32_t)v < c->prm.warp_lg) return fail(c, DIM3G_ERR_INVALID, "block_slots_log2 below warp_slots_log2");
+        c->prm.block_lg = (uint32_t)v;
+    } else if (!strcmp(name, "tile_bits_log2")) {
+        if (v < 10 || v > 20) return fail(c, DIM3G_ERR_INVALID, "tile_bits_log2 must be in 10..20");
+        c->prm.tile_lg = (uint32_t)v;
+    } else if (!strcmp(name, "heavy_min_len")) {
+        if (v < 0) return fail(c, DIM3G_ERR_INVALID, "heavy_min_len must be >= 0");
+        c->prm.heavy_min_len = v;
+    } else {
+        return fail(c, DIM3G_ERR_INVALID, "unknown parameter %s", name);
+    }
+    return DIM3G_OK;
+}
+
+int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
+    if (!c || !name || !v) return DIM3G_ERR_INVALID;
+    if (!strcmp(name, "warp_slots_log2")) *v = c->prm.warp_lg;
+    else if (!strcmp(name, "block_slots_log2")) *v = c->prm.block_lg;
+    else if (!strcmp(name, "tile_bits_log2")) *v = c->prm.tile_lg;
+    else if (!strcmp(name, "heavy_min_len")) *v = c->prm.heavy_min_len;
+    else return DIM3G_ERR_INVALID;
+    return DIM3G_OK;
+}
+
+int dim3g_trim(dim3g_ctx* c) {
+    if (!c) return DIM3G_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->ws.release();
+    if (c->d_in) cudaFree(c->d_in);
+    if (c->d_out) cudaFree(c->d_out);
+    c->d_in = c->d_out = nullptr;
+    c->d_in_bytes = c->d_out_bytes = 0;
+    return DIM3G_OK;
+}
+
+int dim3g_join_project(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, uint64_t nS,
+                       uint32_t** out_xz, uint64_t* n_out) {
+    if (!out_xz) return fail(c, DIM3G_ERR_INVALID, "null output pointer");
+    return host_join(c, R, nR, S, nS, false, out_xz, nullptr, nullptr, 0, n_out);
+}
+
+int dim3g_join_project_into(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, uint64_t nS,
+                            uint32_t* out_xz, uint64_t capacity, uint64_t* n_out) {
+    if (!out_xz) return fail(c, DIM3G_ERR_INVALID, "null output buffer");
+    return host_join(c, R, nR, S, nS, false, nullptr, nullptr, out_xz, capacity, n_out);
+}
+
+int dim3g_join_project_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
+                              uint32_t* d_out, uint64_t capacity, uint64_t* n_out) {
+    if (!c || !n_out || (nR && !dR) || (nS && !dS) || (capacity && !d_out))
+        return fail(c, DIM3G_ERR_INVALID, "null argument");
+    if (!aligned8(dR) || !aligned8(dS) || !aligned8(d_out)) return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
+    CU(cudaSetDevice(c->device));
+    const bool swap = nR < nS;
+    DeviceOut d{(uint2*)d_out, nullptr, capacity};
+    JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
+                swap, false, false, OutPrep{prep_device, &d}};
+    return run_join(c, jp, n_out);
+}
+
+int dim3g_join_project_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
+                                    uint64_t* n_out) {
+    if (!c || !n_out || (nR && !dR) || (nS && !dS)) return fail(c, DIM3G_ERR_INVALID, "null argument");
+    if (!aligned8(dR) || !aligned8(dS)) return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
+    CU(cudaSetDevice(c->device));
+    const bool swap = nR < nS;
+    DeviceOut d{nullptr, nullptr, 0};
+    JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
+                swap, false, true, OutPrep{prep_device, &d}};
+    return run_join(c, jp, n_out);
+}
+
+int dim3g_join_count(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, uint64_t nS,
+                     uint32_t** out_xz, uint64_t** out_cnt, uint64_t* n_out) {
+    if (!out_xz || !out_cnt) return fail(c, DIM3G_ERR_INVALID, "null output pointer");
+    return host_join(c, R, nR, S, nS, true, out_xz, out_cnt, nullptr, 0, n_out);
+}
+
+int dim3g_join_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
+                            uint32_t* d_out_xz, uint64_t* d_out_cnt, uint64_t capacity, uint64_t* n_out) {
+    if (!c || !n_out || (nR && !dR) || (nS && !dS) || (capacity && (!d_out_xz || !d_out_cnt)))
+        return fail(c, DIM3G_ERR_INVALID, "null argument");
+    if (!aligned8(dR) || !aligned8(dS) || !aligned8(d_out_xz) || !aligned8(d_out_cnt))
+        return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
+    CU(cudaSetDevice(c->device));
+    const bool swap = nR < nS;
+    DeviceOut d{(uint2*)d_out_xz, (unsigned long long*)d_out_cnt, capacity};
+    JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
+                swap, true, false, OutPrep{prep_device, &d}};
+    return run_join(c, jp, n_out);
+}
+
+}  // extern "C"
+
+// ========================================================= L+S mapper ABI
+namespace {
+
+int mapper_stage(dim3g_mapper* m, const uint32_t* keys, uint64_t n, uint32_t** dkeys, int32_t** dids) {
+    dim3g_ctx* c = m->ctx;
+    c->ws.reset();
+    *dkeys = ws_get<uint32_t>(c, n);
+    *dids = ws_get<int32_t>(c, n);
+    if (!*dkeys || !*dids) return fail(c, DIM3G_ERR_NOMEM, "mapper staging allocation failed");
+    CU(cudaMemcpyAsync(*dkeys, keys, n * 4, cudaMemcpyHostToDevice, c->stream));
+    return DIM3G_OK;
+}
+
+int mapper_reserve(dim3g_mapper* m, uint64_t want_keys) {
+    dim3g_ctx* c = m->ctx;
+    uint64_t need = next_pow2(want_keys * 2 < 1024 ? 1024 : want_keys * 2);
+    if (need <= m->cap) return DIM3G_OK;
+    unsigned long long* ns = nullptr;
+    if (cudaMalloc(&ns, need * 8) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, DIM3G_ERR_NOMEM, "mapper table allocation failed");
+    }
+    CU(cudaMemsetAsync(ns, 0xff, need * 8, c->stream));
+    if (m->slots) {
+        uint32_t* err = ws_get<uint32_t>(c, 1);
+        if (!err) return fail(c, DIM3G_ERR_NOMEM, "mapper scratch allocation failed");
+        CU(cudaMemsetAsync(err, 0, 4, c->stream));
+        k_mapper_rehash<<<grid_for(m->cap, c->sm_count), 256, 0, c->stream>>>(DevTable{m->slots, m->cap - 1},
+                                                                             DevTable{ns, need - 1}, err);
+        CHECK_LAUNCH();
+        CU(cudaStreamSynchronize(c->stream));
+        cudaFree(m->slots);
+    }
+    m->slots = ns;
+    m->cap = need;
+    return DIM3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dim3g_mapper_create(dim3g_ctx* c, uint64_t hint, dim3g_mapper** out) {
+    if (!c || !out) return DIM3G_ERR_INVALID;
+    *out = nullptr;
+    CU(cudaSetDevice(c->device));
+    dim3g_mapper* m = new dim3g_mapper();
+    m->ctx = c;
+    int r = mapper_reserve(m, hint);
+    if (r) {
+        delete m;
+        return r;
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    *out = m;
+    return DIM3G_OK;
+}
+
+void dim3g_mapper_destroy(dim3g_mapper* m) {
+    if (!m) return;
+    cudaSetDevice(m->ctx->device);
+    cudaStreamSynchronize(m->ctx->stream);
+    if (m->slots) cudaFree(m->slots);
+    delete m;
+}
+
+int dim3g_mapper_insert(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32_t* ids) {
+    if (!m) return DIM3G_ERR_INVALID;
+    dim3g_ctx* c = m->ctx;
+    if ((n && (!keys || !ids)) || n >= 0x7FFFFFFFull) return fail(c, DIM3G_ERR_INVALID, "bad mapper batch");
+    if (n == 0) return DIM3G_OK;
+    if (m->cnt + (int64_t)n >= 0x7FFFFFFFll) return fail(c, DIM3G_ERR_UNSUPPORTED, "mapper id space exhausted");
+    CU(cudaSetDevice(c->device));
+    int r = mapper_reserve(m, (uint64_t)m->nkeys + n);
+    if (r) return r;
+    uint32_t* dk;
+    int32_t* di;
+    if ((r = mapper_stage(m, keys, n, &dk, &di))) return r;
+    uint64_t* bsum = ws_get<uint64_t>(c, scan_blocks(n) + 1);
+    unsigned long long* total = ws_get<unsigned long long>(c, 1);
+    uint32_t* err = ws_get<uint32_t>(c, 1);
+    if (!bsum || !total || !err) return fail(c, DIM3G_ERR_NOMEM, "mapper scratch allocation failed");
+    cudaStream_t st = c->stream;
+    DevTable t{m->slots, m->cap - 1};
+    CU(cudaMemsetAsync(err, 0, 4, st));
+    k_mapper_claim<<<grid_for(n, c->sm_count), 256, 0, st>>>(t, dk, n, err);
+    CHECK_LAUNCH();
+    device_scan(FirstOccSrc{t, dk}, AssignNewIdDst{t, dk, (long long)m->cnt}, n, bsum, total, st);
+    k_mapper_gather<<<grid_for(n, c->sm_count), 256, 0, st>>>(t, dk, n, di);
+    CHECK_LAUNCH();
+    unsigned long long h_total = 0;
+    uint32_t h_err = 0;
+    CU(cudaMemcpyAsync(ids, di, n * 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&h_total, total, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (h_err) return fail(c, DIM3G_ERR_DEVICE, "mapper probe bound violated");
+    m->cnt += (int64_t)h_total;
+    m->nkeys += (int64_t)h_total;
+    return DIM3G_OK;
+}
+
+int dim3g_mapper_find(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32_t* ids) {
+    if (!m) return DIM3G_ERR_INVALID;
+    dim3g_ctx* c = m->ctx;
+    if (n && (!keys || !ids)) return fail(c, DIM3G_ERR_INVALID, "bad mapper batch");
+    if (n == 0) return DIM3G_OK;
+    CU(cudaSetDevice(c->device));
+    uint32_t* dk;
+    int32_t* di;
+    int r = mapper_stage(m, keys, n, &dk, &di);
+    if (r) return r;
+    k_mapper_find<<<grid_for(n, c->sm_count), 256, 0, c->stream>>>(DevTable{m->slots, m->cap - 1}, dk, n, di);
+    CHECK_LAUNCH();
+    CU(cudaMemcpyAsync(ids, di, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return DIM3G_OK;
+}
+
+int64_t dim3g_mapper_size(const dim3g_mapper* m) { return m ? m->cnt : -1; }
+
+int dim3g_mapper_clear(dim3g_mapper* m) {
+    if (!m) return DIM3G_ERR_INVALID;
+    dim3g_ctx* c = m->ctx;
+    CU(cudaSetDevice(c->device));
+    CU(cudaMemsetAsync(m->slots, 0xff, m->cap * 8, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    m->nkeys = 0;
+    return DIM3G_OK;
+}
+
+int dim3g_mapper_set_cnt(dim3g_mapper* m, int64_t cnt) {
+    if (!m || cnt < 0 || cnt >= 0x7FFFFFFFll) return DIM3G_ERR_INVALID;
+    m->cnt = cnt;
+    return DIM3G_OK;
+}
+
+}  // extern "C"

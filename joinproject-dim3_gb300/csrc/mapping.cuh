@@ -1,0 +1,160 @@
+// mapping.cuh -- value -> dense id mapping on the GPU (the role of the
+// reference's mapping_step + LS_mapper, dim3.hpp:394-883 and
+// Include/L+S_mapper.hpp:11-160), plus the CSR builds (divide_R
+// dim3.hpp:1058-1086, the sparse half of divide_S dim3.hpp:1186-1253).
+//
+// Table layout: one 64-bit slot per entry, key in the high half, dense id in
+// the low half; the all-ones word marks an empty slot, so every 32-bit key
+// (0xFFFFFFFF included) is a valid key.  Open addressing with linear probing
+// at load factor <= 1/2; ids are assigned after the build by a prefix sum
+// over occupied slots, so they are dense in [0, count).
+#pragma once
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace dim3g {
+
+constexpr uint32_t kNotFound = 0xFFFFFFFFu;
+
+struct DevTable {
+    unsigned long long* slots;
+    uint64_t mask;  // capacity - 1 (capacity is a power of two)
+};
+
+__device__ __forceinline__ bool table_insert(DevTable t, uint32_t key, uint32_t* err) {
+    uint64_t h = mix32(key) & t.mask;
+    const unsigned long long want = (unsigned long long)key << 32;
+    for (uint64_t p = 0; p <= t.mask; p++) {
+        unsigned long long cur = __ldcg(&t.slots[h]);
+        if (cur == kEmpty64) {
+            unsigned long long prev = atomicCAS(&t.slots[h], (unsigned long long)kEmpty64, want);
+            if (prev == kEmpty64) return true;
+            cur = prev;
+        }
+        if ((uint32_t)(cur >> 32) == key) return false;
+        h = (h + 1) & t.mask;
+    }
+    raise_error(err, kErrProbeLimit);
+    return false;
+}
+
+__device__ __forceinline__ uint32_t table_find(DevTable t, uint32_t key) {
+    uint64_t h = mix32(key) & t.mask;
+    for (uint64_t p = 0; p <= t.mask; p++) {
+        unsigned long long cur = __ldg(&t.slots[h]);
+        if (cur == kEmpty64) return kNotFound;
+        if ((uint32_t)(cur >> 32) == key) return (uint32_t)cur;
+        h = (h + 1) & t.mask;
+    }
+    return kNotFound;
+}
+
+// Build pass over the larger relation P: insert its first column into tx and
+// its y column into ty.
+__global__ void k_insert_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint32_t* err) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 p = P[i];
+        table_insert(tx, p.x, err);
+        table_insert(ty, p.y, err);
+    }
+}
+
+// Semi-join of Q against ty (mapping_y's probe, dim3.hpp:816-827): keep the
+// tuples whose y occurs in P as (c, y id), insert their first column into tz.
+__global__ void k_probe_q(const uint2* __restrict__ Q, uint64_t n, DevTable ty, DevTable tz, uint2* __restrict__ Qk,
+                          unsigned long long* nkept, uint32_t* err) {
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = i0 + threadIdx.x;
+        bool keep = false;
+        uint2 q = make_uint2(0, 0);
+        uint32_t yid = kNotFound;
+        if (i < n) {
+            q = Q[i];
+            yid = table_find(ty, q.y);
+            keep = (yid != kNotFound);
+            if (keep) table_insert(tz, q.x, err);
+        }
+        uint32_t b = __ballot_sync(0xffffffffu, keep);
+        if (b) {
+            unsigned long long base = 0;
+            int leader = __ffs(b) - 1;
+            if ((int)lane_id() == leader) base = atomicAdd(nkept, (unsigned long long)__popc(b));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (keep) Qk[base + __popc(b & lanemask_lt())] = make_uint2(q.x, yid);
+        }
+    }
+}
+
+// Table compaction: ids by prefix sum over occupied slots.
+struct OccupiedSrc {
+    const unsigned long long* slots;
+    __device__ uint64_t operator()(uint64_t i) const { return slots[i] != kEmpty64 ? 1u : 0u; }
+};
+struct AssignIdDst {
+    unsigned long long* slots;
+    uint32_t* id2v;
+    __device__ void operator()(uint64_t i, uint64_t e, uint64_t v) const {
+        if (!v) return;
+        unsigned long long s = slots[i];
+        uint32_t key = (uint32_t)(s >> 32);
+        slots[i] = ((unsigned long long)key << 32) | (uint32_t)e;
+        if (id2v) id2v[e] = key;
+    }
+};
+
+// P -> (x id, y id); per-x degree histogram.
+__global__ void k_map_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint2* __restrict__ Pm,
+                        uint32_t* __restrict__ degx) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 p = P[i];
+        uint32_t xi = table_find(tx, p.x);
+        uint32_t yi = table_find(ty, p.y);
+        Pm[i] = make_uint2(xi, yi);
+        atomicAdd(&degx[xi], 1u);
+    }
+}
+
+// Q' -> (z id, y id); histogram over the (y, z tile) CSR key y*T + z/TB.
+__global__ void k_map_q(uint2* __restrict__ Qk, uint64_t n, DevTable tz, uint32_t T, uint32_t tile_shift,
+                        uint32_t* __restrict__ cnt_yt) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 q = Qk[i];
+        uint32_t zi = table_find(tz, q.x);
+        Qk[i] = make_uint2(zi, q.y);
+        atomicAdd(&cnt_yt[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
+    }
+}
+
+// Row pointers from a histogram: JR[i] = cursor[i] = exclusive prefix.
+struct U32Src {
+    const uint32_t* a;
+    __device__ uint64_t operator()(uint64_t i) const { return a[i]; }
+};
+struct RowPtrDst {
+    uint32_t* jr;
+    uint32_t* cursor;
+    __device__ void operator()(uint64_t i, uint64_t e, uint64_t) const {
+        jr[i] = (uint32_t)e;
+        cursor[i] = (uint32_t)e;
+    }
+};
+
+__global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uint32_t* __restrict__ cursor,
+                            uint32_t* __restrict__ ic) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 p = Pm[i];
+        uint32_t pos = atomicAdd(&cursor[p.x], 1u);
+        ic[pos] = p.y;
+    }
+}
+
+__global__ void k_scatter_s(const uint2* __restrict__ Qm, uint64_t n, uint32_t T, uint32_t tile_shift,
+                            uint32_t* __restrict__ cursor, uint32_t* __restrict__ ic) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 q = Qm[i];
+        uint32_t pos = atomicAdd(&cursor[(uint64_t)q.y * T + (q.x >> tile_shift)], 1u);
+        ic[pos] = q.x;
+    }
+}
+
+}  // namespace dim3g

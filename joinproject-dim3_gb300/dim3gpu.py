@@ -1,0 +1,342 @@
+"""Python binding of the GB300 join-project library (ctypes over the C ABI
+declared in include/dim3gpu.h).
+
+The binding mirrors the reference's entry points:
+
+    DIM3::doJoinProject(R, S, result)          -> Context.join_project(R, S)
+    DIM3_parallel::doJoinProject_parallel(...) -> Context.join_project(R, S)
+    DIM3JoinAggregate::doJoinAggregate (COUNT) -> Context.join_count(R, S)
+    LS_mapper insert / find / size / clear     -> Mapper
+
+Relations are (n, 2) uint32 arrays (x, y) / (z, y).  There is no CPU
+fallback: loading fails loudly when the CUDA library is absent.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdim3gpu.so")
+GEN_PATH = os.path.join(HERE, "libdim3gen.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_DEVICE, ERR_UNSUPPORTED = range(7)
+_NAMES = {1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "CAPACITY", 5: "DEVICE", 6: "UNSUPPORTED"}
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class Dim3GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("dim3g error %s (%d): %s" % (_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("n_big", ctypes.c_uint64), ("n_small", ctypes.c_uint64), ("n_small_kept", ctypes.c_uint64),
+        ("out_j", ctypes.c_uint64), ("n_out", ctypes.c_uint64),
+        ("swapped", ctypes.c_uint32), ("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("nz", ctypes.c_uint32),
+        ("rows_warp", ctypes.c_uint32), ("rows_block", ctypes.c_uint32), ("rows_bitmap", ctypes.c_uint32),
+        ("rows_dense", ctypes.c_uint32), ("z_tiles", ctypes.c_uint32), ("heavy_y", ctypes.c_uint32),
+        ("ms_map", ctypes.c_float), ("ms_csr", ctypes.c_float), ("ms_count", ctypes.c_float),
+        ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every symbol include/dim3gpu.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "dim3g_create", "dim3g_destroy", "dim3g_set_stream", "dim3g_last_error", "dim3g_get_stats",
+    "dim3g_set_param", "dim3g_get_param", "dim3g_trim",
+    "dim3g_join_project", "dim3g_join_project_into", "dim3g_join_project_device",
+    "dim3g_join_project_count_device", "dim3g_join_count", "dim3g_join_count_device",
+    "dim3g_mapper_create", "dim3g_mapper_destroy", "dim3g_mapper_insert", "dim3g_mapper_find",
+    "dim3g_mapper_size", "dim3g_mapper_clear", "dim3g_mapper_set_cnt",
+]
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("libdim3gpu.so not built (run __graft_entry__.build()): " + path)
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    L.dim3g_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+    L.dim3g_destroy.argtypes = [vp]
+    L.dim3g_destroy.restype = None
+    L.dim3g_set_stream.argtypes = [vp, vp]
+    L.dim3g_last_error.argtypes = [vp]
+    L.dim3g_last_error.restype = ctypes.c_char_p
+    L.dim3g_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.dim3g_set_param.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
+    L.dim3g_get_param.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
+    L.dim3g_trim.argtypes = [vp]
+    L.dim3g_join_project.argtypes = [vp, _u32p, ctypes.c_uint64, _u32p, ctypes.c_uint64, ctypes.POINTER(_u32p), _u64p]
+    L.dim3g_join_project_into.argtypes = [vp, _u32p, ctypes.c_uint64, _u32p, ctypes.c_uint64, _u32p,
+                                          ctypes.c_uint64, _u64p]
+    L.dim3g_join_project_device.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, vp, ctypes.c_uint64, _u64p]
+    L.dim3g_join_project_count_device.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, _u64p]
+    L.dim3g_join_count.argtypes = [vp, _u32p, ctypes.c_uint64, _u32p, ctypes.c_uint64, ctypes.POINTER(_u32p),
+                                   ctypes.POINTER(_u64p), _u64p]
+    L.dim3g_join_count_device.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, vp, vp, ctypes.c_uint64,
+                                          _u64p]
+    L.dim3g_mapper_create.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.dim3g_mapper_destroy.argtypes = [vp]
+    L.dim3g_mapper_destroy.restype = None
+    L.dim3g_mapper_insert.argtypes = [vp, _u32p, ctypes.c_uint64, _i32p]
+    L.dim3g_mapper_find.argtypes = [vp, _u32p, ctypes.c_uint64, _i32p]
+    L.dim3g_mapper_size.argtypes = [vp]
+    L.dim3g_mapper_size.restype = ctypes.c_int64
+    L.dim3g_mapper_clear.argtypes = [vp]
+    L.dim3g_mapper_set_cnt.argtypes = [vp, ctypes.c_int64]
+    _lib = L
+    return L
+
+
+_libc = ctypes.CDLL(None)
+_libc.free.argtypes = [ctypes.c_void_p]
+
+
+def _pairs(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32).reshape(-1, 2)
+    return a, a.ctypes.data_as(_u32p), a.shape[0]
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor or an int."""
+    return ctypes.c_void_p(t if isinstance(t, int) else t.data_ptr())
+
+
+class Context:
+    """One GPU context: a stream, a workspace and the last call's stats."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        self.h = ctypes.c_void_p()
+        rc = self.L.dim3g_create(device, ctypes.byref(self.h))
+        if rc != OK:
+            raise Dim3GError(rc, "dim3g_create failed for device %d" % device)
+
+    def close(self):
+        if self.h:
+            self.L.dim3g_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != OK:
+            raise Dim3GError(rc, self.L.dim3g_last_error(self.h).decode(errors="replace"))
+
+    def set_stream(self, stream_handle):
+        self._check(self.L.dim3g_set_stream(self.h, ctypes.c_void_p(stream_handle or None)))
+
+    def set_param(self, name, value):
+        self._check(self.L.dim3g_set_param(self.h, name.encode(), int(value)))
+
+    def get_param(self, name):
+        v = ctypes.c_int64()
+        self._check(self.L.dim3g_get_param(self.h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.dim3g_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def trim(self):
+        self._check(self.L.dim3g_trim(self.h))
+
+    # -------------------------------------------------------- join-project
+    def join_project(self, R, S):
+        """Host arrays in, (n, 2) uint32 distinct pairs out (DIM3::doJoinProject)."""
+        R, rp, nr = _pairs(R)
+        S, sp, ns = _pairs(S)
+        out = _u32p()
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_project(self.h, rp, nr, sp, ns, ctypes.byref(out), ctypes.byref(n)))
+        try:
+            if n.value == 0:
+                return np.zeros((0, 2), dtype=np.uint32)
+            return np.ctypeslib.as_array(out, shape=(n.value * 2,)).copy().reshape(-1, 2)
+        finally:
+            _libc.free(ctypes.cast(out, ctypes.c_void_p))
+
+    def join_project_into(self, R, S, out):
+        """Host arrays in; pairs into the caller's (capacity, 2) uint32 array."""
+        R, rp, nr = _pairs(R)
+        S, sp, ns = _pairs(S)
+        assert out.dtype == np.uint32 and out.flags["C_CONTIGUOUS"]
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_project_into(self.h, rp, nr, sp, ns, out.ctypes.data_as(_u32p),
+                                                   out.size // 2, ctypes.byref(n)))
+        return n.value
+
+    def join_project_device(self, dR, nR, dS, nS, dout, capacity):
+        """Device pointers (ints or torch tensors) in and out; returns the pair count."""
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_project_device(self.h, _ptr(dR), nR, _ptr(dS), nS, _ptr(dout), capacity,
+                                                     ctypes.byref(n)))
+        return n.value
+
+    def join_project_count_device(self, dR, nR, dS, nS):
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_project_count_device(self.h, _ptr(dR), nR, _ptr(dS), nS, ctypes.byref(n)))
+        return n.value
+
+    # ------------------------------------------------------ join-aggregate
+    def join_count(self, R, S):
+        """COUNT(*) GROUP BY (x, z): returns ((n, 2) uint32 pairs, (n,) uint64 counts)."""
+        R, rp, nr = _pairs(R)
+        S, sp, ns = _pairs(S)
+        oxz = _u32p()
+        oc = _u64p()
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_count(self.h, rp, nr, sp, ns, ctypes.byref(oxz), ctypes.byref(oc),
+                                            ctypes.byref(n)))
+        try:
+            if n.value == 0:
+                return np.zeros((0, 2), dtype=np.uint32), np.zeros(0, dtype=np.uint64)
+            pairs = np.ctypeslib.as_array(oxz, shape=(n.value * 2,)).copy().reshape(-1, 2)
+            cnt = np.ctypeslib.as_array(oc, shape=(n.value,)).copy()
+            return pairs, cnt
+        finally:
+            _libc.free(ctypes.cast(oxz, ctypes.c_void_p))
+            _libc.free(ctypes.cast(oc, ctypes.c_void_p))
+
+    def join_count_device(self, dR, nR, dS, nS, dout_xz, dout_cnt, capacity):
+        n = ctypes.c_uint64()
+        self._check(self.L.dim3g_join_count_device(self.h, _ptr(dR), nR, _ptr(dS), nS, _ptr(dout_xz),
+                                                   _ptr(dout_cnt), capacity, ctypes.byref(n)))
+        return n.value
+
+
+class Mapper:
+    """GPU L+S mapper: value -> dense id with the reference's insert order."""
+
+    def __init__(self, ctx, capacity_hint=1024):
+        self.ctx = ctx
+        self.L = ctx.L
+        self.h = ctypes.c_void_p()
+        ctx._check(self.L.dim3g_mapper_create(ctx.h, capacity_hint, ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.L.dim3g_mapper_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _batch(self, fn, keys):
+        k = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1)
+        ids = np.empty(k.shape[0], dtype=np.int32)
+        self.ctx._check(fn(self.h, k.ctypes.data_as(_u32p), k.shape[0], ids.ctypes.data_as(_i32p)))
+        return ids
+
+    def insert(self, keys):
+        return self._batch(self.L.dim3g_mapper_insert, keys)
+
+    def find(self, keys):
+        return self._batch(self.L.dim3g_mapper_find, keys)
+
+    def size(self):
+        return self.L.dim3g_mapper_size(self.h)
+
+    def clear(self):
+        self.ctx._check(self.L.dim3g_mapper_clear(self.h))
+
+    def set_cnt(self, v):
+        self.ctx._check(self.L.dim3g_mapper_set_cnt(self.h, int(v)))
+
+
+# ------------------------------------------------------------ generators
+_gen = None
+
+
+def gen():
+    global _gen
+    if _gen is None:
+        if not os.path.exists(GEN_PATH):
+            raise OSError("libdim3gen.so not built: " + GEN_PATH)
+        G = ctypes.CDLL(GEN_PATH)
+        G.dim3gen_minstd.argtypes = [ctypes.c_uint32] * 6 + [_u32p, _u32p]
+        G.dim3gen_zipf_side.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                                        ctypes.c_uint64, _u32p]
+        G.dim3gen_chung_lu.argtypes = [ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, _u32p,
+                                       _u32p]
+        G.dim3gen_chung_lu.restype = ctypes.c_uint64
+        G.dim3gen_batch_params.argtypes = [ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_double] * 6 + [
+            _u64p, ctypes.POINTER(ctypes.c_double), _u32p]
+        G.dim3gen_rank_value.argtypes = [ctypes.c_uint32]
+        G.dim3gen_rank_value.restype = ctypes.c_uint32
+        _gen = G
+    return _gen
+
+
+def gen_rand_data(nR=10 ** 7, nS=10 ** 7, modx=10 ** 6, mody=10 ** 6, modz=10 ** 6, seed=492):
+    """The reference's gen_rand_data (dim3.hpp:1556-1568), bit-identical."""
+    R = np.empty((nR, 2), dtype=np.uint32)
+    S = np.empty((nS, 2), dtype=np.uint32)
+    gen().dim3gen_minstd(nR, nS, modx, mody, modz, seed, R.ctypes.data_as(_u32p), S.ctypes.data_as(_u32p))
+    return R, S
+
+
+def zipf_side(n, dom_a, dom_b, s, seed):
+    out = np.empty((n, 2), dtype=np.uint32)
+    if gen().dim3gen_zipf_side(n, dom_a, dom_b, s, seed, out.ctypes.data_as(_u32p)) != 0:
+        raise MemoryError("zipf generator failed")
+    return out
+
+
+def chung_lu(n=1 << 21, beta=2.1, M=10 ** 7, seed=7):
+    buf = np.empty((2 * M, 2), dtype=np.uint32)
+    mw = ctypes.c_uint32()
+    k = gen().dim3gen_chung_lu(n, beta, M, seed, buf.ctypes.data_as(_u32p), ctypes.byref(mw))
+    return buf[:k]
+
+
+def batch_params(seed, q, n_lo=1e4, n_hi=4e6, s_lo=0.5, s_hi=1.5, d_lo=1e3, d_hi=1e6):
+    n = ctypes.c_uint64()
+    s = ctypes.c_double()
+    d = ctypes.c_uint32()
+    gen().dim3gen_batch_params(seed, q, n_lo, n_hi, s_lo, s_hi, d_lo, d_hi, ctypes.byref(n), ctypes.byref(s),
+                               ctypes.byref(d))
+    return n.value, s.value, d.value
+
+
+# Named workloads (the bench and the tests use the same shapes).
+def workload(name, scale=1.0):
+    """Seeded synthetic relations by name; scale < 1 shrinks tuple counts."""
+    if name == "zipf_1m":  # 1M tuples per side, dom(A)=dom(C)=50k, dom(B)=20k Zipf s=1.0
+        n = max(1, int(10 ** 6 * scale))
+        return zipf_side(n, 50000, 20000, 1.0, 101), zipf_side(n, 50000, 20000, 1.0, 202)
+    if name == "chung_lu_20m":  # self join of a 2^21-vertex Chung-Lu graph, ~20M directed edges
+        M = max(1, int(10 ** 7 * scale))
+        nv = 1 << 21 if scale >= 1 else max(1024, int((1 << 21) * scale))
+        E = chung_lu(nv, 2.1, M, 7)
+        return E, E
+    if name == "zipf12_16m":  # 16M tuples per side, dom(A)=dom(C)=1M, dom(B)=200k Zipf s=1.2
+        n = max(1, int(16 * 10 ** 6 * scale))
+        return zipf_side(n, 10 ** 6, 200000, 1.2, 303), zipf_side(n, 10 ** 6, 200000, 1.2, 404)
+    if name == "gen_rand_data":
+        n = max(1, int(10 ** 7 * scale))
+        return gen_rand_data(n, n, 10 ** 6, 10 ** 6, 10 ** 6, 492)
+    raise KeyError(name)

@@ -1,0 +1,142 @@
+"""GPU parity: the CUDA path against the reference's golden fixtures, through
+the C ABI (host and device entry points), plus the edge cases the reference
+exercises (empty inputs, no matches, swap, duplicates, extreme keys)."""
+import numpy as np
+import pytest
+
+from helpers import case_inputs, check_groups, check_pairs
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["empty_R", "empty_S", "no_match", "single", "extreme_keys", "heavy_duplicates", "one_join_value",
+         "grd_tiny", "grd_swap_dense", "grd_small", "grd_classical", "grd_dense_z", "grd_swap", "grd_sparse",
+         "grd_all_dense", "zipf_1m_s001", "zipf_1m_s01", "chung_lu_s0005", "chung_lu_s005"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_join_project_host_api(ctx, golden, name):
+    index, arrays = golden
+    R, S = case_inputs(name, index, arrays)
+    got = ctx.join_project(R, S)
+    check_pairs(got, index[name], arrays, name)
+    st = ctx.stats()
+    assert st["n_out"] == index[name]["n_out"]
+    assert st["swapped"] == (1 if R.shape[0] < S.shape[0] else 0)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_join_count_host_api(ctx, golden, name):
+    index, arrays = golden
+    R, S = case_inputs(name, index, arrays)
+    pairs, cnt = ctx.join_count(R, S)
+    check_groups(pairs, cnt, index[name], arrays, name)
+
+
+@pytest.mark.parametrize("name", ["grd_small", "grd_swap", "chung_lu_s005", "zipf_1m_s001"])
+def test_join_project_device_api(ctx, golden, name):
+    import torch
+    index, arrays = golden
+    R, S = case_inputs(name, index, arrays)
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    n_need = index[name]["n_out"]
+    # too small a buffer: CAPACITY with the size needed, nothing written
+    import dim3gpu
+    small = torch.full((max(1, n_need // 2), 2), -1, dtype=torch.int32, device="cuda")
+    if n_need > 1:
+        with pytest.raises(dim3gpu.Dim3GError) as e:
+            ctx.join_project_device(dR, R.shape[0], dS, S.shape[0], small, small.shape[0])
+        assert e.value.code == dim3gpu.ERR_CAPACITY
+        assert bool((small == -1).all())
+    assert ctx.join_project_count_device(dR, R.shape[0], dS, S.shape[0]) == n_need
+    out = torch.empty((n_need + 5, 2), dtype=torch.int32, device="cuda")
+    n = ctx.join_project_device(dR, R.shape[0], dS, S.shape[0], out, out.shape[0])
+    torch.cuda.synchronize()
+    got = out[:n].cpu().numpy().view(np.uint32)
+    check_pairs(got, index[name], arrays, name)
+
+
+def test_join_count_device_api(ctx, golden):
+    import torch
+    index, arrays = golden
+    name = "grd_dense_z"
+    R, S = case_inputs(name, index, arrays)
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    n_need = index[name]["n_groups"]
+    oxz = torch.empty((n_need, 2), dtype=torch.int32, device="cuda")
+    oc = torch.empty((n_need,), dtype=torch.int64, device="cuda")
+    n = ctx.join_count_device(dR, R.shape[0], dS, S.shape[0], oxz, oc, n_need)
+    torch.cuda.synchronize()
+    check_groups(oxz[:n].cpu().numpy().view(np.uint32), oc[:n].cpu().numpy().view(np.uint64), index[name],
+                 arrays, name)
+
+
+@pytest.mark.parametrize("params", [
+    {"warp_slots_log2": 5, "block_slots_log2": 8, "tile_bits_log2": 10},
+    {"warp_slots_log2": 8, "block_slots_log2": 10, "tile_bits_log2": 12},
+    {"warp_slots_log2": 11, "block_slots_log2": 14, "tile_bits_log2": 20},
+])
+def test_kernel_classes_and_tiling_agree(built, golden, params):
+    """Every row class and z tiling gives the same answer (forces rows through
+    the bitmap class with many z tiles, or through the hash classes)."""
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    for k, v in params.items():
+        c.set_param(k, v)
+    for name in ["grd_small", "grd_sparse", "chung_lu_s005", "zipf_1m_s001"]:
+        R, S = case_inputs(name, index, arrays)
+        check_pairs(c.join_project(R, S), index[name], arrays, name)
+        p, cnt = c.join_count(R, S)
+        check_groups(p, cnt, index[name], arrays, name)
+    c.close()
+
+
+def test_repeated_calls_are_stable(ctx, golden):
+    index, arrays = golden
+    R, S = case_inputs("chung_lu_s005", index, arrays)
+    for _ in range(3):
+        check_pairs(ctx.join_project(R, S), index["chung_lu_s005"], arrays, "chung_lu_s005")
+
+
+def test_bad_params_rejected(ctx):
+    import dim3gpu
+    with pytest.raises(dim3gpu.Dim3GError):
+        ctx.set_param("warp_slots_log2", 40)
+    with pytest.raises(dim3gpu.Dim3GError):
+        ctx.set_param("no_such_knob", 1)
+
+
+def test_mapper_matches_sequential_insert_semantics(ctx):
+    """GPU L+S mapper: ids equal those of a sequential LS_mapper insert loop."""
+    import dim3gpu
+    rng = np.random.default_rng(3)
+    m = dim3gpu.Mapper(ctx, 16)
+    ref = {}
+    cnt = 0
+    for batch in range(4):
+        keys = rng.integers(0, 5000, size=20000, dtype=np.uint64).astype(np.uint32)
+        if batch == 2:
+            keys[:5] = [0xFFFFFFFF, 0, 0xFFFFFFFF, 7, 0]
+        ids = m.insert(keys)
+        want = np.empty_like(ids)
+        for i, k in enumerate(keys.tolist()):
+            if k not in ref:
+                ref[k] = cnt
+                cnt += 1
+            want[i] = ref[k]
+        assert np.array_equal(ids, want)
+        assert m.size() == cnt
+    probe = np.array([0xFFFFFFFF, 0, 123456789, 7], dtype=np.uint32)
+    f = m.find(probe)
+    assert f.tolist() == [ref.get(int(k), -1) for k in probe]
+    m.clear()
+    assert (m.find(probe) == -1).all()
+    assert m.size() == cnt  # clear() keeps the counter (L+S_mapper.hpp:37-40)
+    ids = m.insert(np.array([5, 6, 5], dtype=np.uint32))
+    assert ids.tolist() == [cnt, cnt + 1, cnt]
+    m.set_cnt(0)
+    m.clear()
+    assert m.insert(np.array([9], dtype=np.uint32)).tolist() == [0]
+    m.close()
