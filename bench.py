@@ -1,0 +1,285 @@
+"""Benchmark: distinct (a,c) Mpairs/s of the GB300 join-project path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+                    [--workload chung_lu_20m|zipf_1m]
+
+Workload (default): self join-project of an undirected Chung-Lu power-law
+graph, 2^21 vertices, degree exponent 2.1, 1e7 edge samples -> ~20M directed
+uint32 edges, R = S (distinct 2-hop neighbours).  Synthetic, seeded.
+
+A step is one join-project call over the resident relations.  `value` times
+K device-resident steps (inputs and output buffer in HBM) with CUDA events on
+the library's stream; `e2e` times K steps through the host-buffer C ABI
+(dim3g_join_project_into): H2D of R and S from pinned memory, the join, and
+D2H of every output pair into pinned memory.  The inputs (320 MB) and the
+output (~87 GB) are far larger than L2, so no flush is needed between steps.
+
+--impl reference times the reference's CPU algorithm (the oracle port of
+DIM3_parallel, all host threads) on a bounded A-slice of the same workload.
+Under torchrun every rank runs an independent replica (the path does not
+exchange data between GPUs); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "joinproject-dim3_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "distinct (a,c) Mpairs/s at 20M-edge 2-hop"
+UNIT = "Mpairs/s"
+WORKLOADS = {
+    "chung_lu_20m": "self join-project, Chung-Lu 2^21 vertices, beta 2.1, 1e7 samples (~20M directed edges)",
+    "zipf_1m": "R,S 1M tuples, dom(A)=dom(C)=50k uniform, dom(B)=20k Zipf s=1.0",
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = None
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 4 + i and s[4 + i] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def make_workload(name):
+    import dim3gpu
+    return dim3gpu.workload(name, 1.0)
+
+
+def a_slice(R, parts, which):
+    """Rows of R whose first value falls in hash bucket `which` of `parts`."""
+    h = (R[:, 0].astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) >> np.uint64(40)
+    return np.ascontiguousarray(R[(h % np.uint64(parts)) == which])
+
+
+def cpu_run(R, S, parts, which, threads):
+    """One oracle DIM3_parallel run on an A-slice; the slice stays the larger
+    input so the output orientation is (a, c)."""
+    from oracle import oracle_py
+    Rs = a_slice(R, parts, which)
+    t = time.perf_counter()
+    # Full S as the first argument keeps it the larger side (no swap of
+    # roles); the pairs are (c, a), the same set transposed.
+    _, n, _, st = oracle_py.join_project(S, Rs, threads=threads, hash_only=False)
+    dt = time.perf_counter() - t
+    return n, dt, st
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    R, S = make_workload(args.workload)
+    parts = args.cpu_parts
+    for w in range(args.warmup):
+        cpu_run(R, S, parts, w % parts, threads)
+    tot_n, tot_t = 0, 0.0
+    for k in range(args.steps):
+        n, dt, st = cpu_run(R, S, parts, (args.warmup + k) % parts, threads)
+        tot_n += n
+        tot_t += dt
+    value = tot_n / tot_t / 1e6
+    sample = "1/%d A-slice of %s per step (full S), oracle port of DIM3_parallel" % (parts, args.workload)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "sample": sample},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(args):
+    threads = os.cpu_count() or 1
+    R, S = make_workload(args.workload)
+    parts = args.cpu_parts
+    n, dt, st = cpu_run(R, S, parts, 0, threads)
+    return {"value": round(n / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "1/%d A-slice of %s (full S): %d pairs in %.2f s; oracle port of DIM3_parallel, %d threads"
+                      % (parts, args.workload, n, dt, threads)}
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import dim3gpu
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    R, S = make_workload(args.workload)
+    nR, nS = R.shape[0], S.shape[0]
+    ctx = dim3gpu.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    n_out = ctx.join_project_count_device(dR, nR, dS, nS)
+    out = torch.empty((n_out, 2), dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        ctx.join_project_device(dR, nR, dS, nS, out, n_out)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ms_write = []
+    ms_phase = {"ms_map": 0.0, "ms_csr": 0.0, "ms_count": 0.0, "ms_write": 0.0}
+    launches0 = ctx.stats()["launches"]
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            n = ctx.join_project_device(dR, nR, dS, nS, out, n_out)
+            st = ctx.stats()
+            ms_write.append(st["ms_write"])
+            for k in ms_phase:
+                ms_phase[k] += st[k]
+        ev1.record(stream)
+        barrier()
+        ms = ev0.elapsed_time(ev1) / args.steps
+    assert n == n_out
+    launches = ctx.stats()["launches"] - launches0
+    clocks = clk.summary()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n_out * world / (ms / 1e3) / 1e6
+
+    # e2e through the host-buffer ABI: pinned R, S and output.
+    e2e = None
+    if args.e2e_steps > 0:
+        hR = torch.from_numpy(R.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        hS = torch.from_numpy(S.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        del out
+        torch.cuda.empty_cache()
+        hout = torch.empty((n_out, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        ctx.join_project_into(hR, hS, hout)  # warm the staging buffers
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            n2 = ctx.join_project_into(hR, hS, hout)
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        assert n2 == n_out
+        if dist is not None:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": round(n_out * world / e2e_s / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int((nR + nS) * 8), "d2h_bytes_per_step": int(n_out * 8),
+               "ms_per_step": round(e2e_s * 1e3, 3)}
+    st = ctx.stats()
+    peak, peak_kind = load_peaks()
+    # Dominant kernel: the write pass of the expansion (one launch per row
+    # class).  Algorithmic bytes per launch: 4 B per candidate read + 8 B per
+    # distinct pair written.
+    ms_w = sum(ms_write) / len(ms_write)
+    alg_bytes = 4 * st["out_j"] + 8 * n_out
+    achieved = alg_bytes / (ms_w / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "nR": int(nR), "nS": int(nS),
+                   "n_out": int(n_out), "out_j": int(st["out_j"]), "l2": "inputs 8(|R|+|S|) and output > L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "phases_ms": {k: round(v / args.steps, 3) for k, v in ms_phase.items()},
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "kernel": "expand write pass (k_rows_warp/block/bitmap<true>)",
+                     "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": args.traffic,
+                     "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(ms_w, 3)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu else None
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="chung_lu_20m", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-parts", type=int, default=64)
+    ap.add_argument("--traffic", type=float, default=None)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -53,6 +53,7 @@ typedef struct {
     float ms_count;            /* device ms: count pass + offsets */
     float ms_write;            /* device ms: write pass */
     float ms_total;            /* device ms: whole call (inputs resident) */
+    uint64_t launches;         /* kernels launched on this context since creation */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */

@@ -4,8 +4,8 @@
 // The count pass is the join-project count pass (distinct z per row).  The
 // write pass expands each row again with a per-z counter -- a shared-memory
 // hash map (z -> count) for classes 1 and 2, a shared-memory counter array
-// over one z tile for class 3 -- and then emits every (x, z, count) of the
-// row at off[x] + a row-local slot.  Counts are exact: each expansion
+// over one z tile for classes 3/4 -- and then emits every (x, z, count) of
+// the row at off[x] + a row-local slot.  Counts are exact: each expansion
 // candidate is one joining (R tuple, S tuple) pair.
 #pragma once
 #include "common.cuh"
@@ -35,9 +35,37 @@ __device__ __forceinline__ uint32_t smem_map_slot(uint32_t* keys, uint32_t lg, u
     return 0xFFFFFFFFu;
 }
 
+// Counting "sets" for warp_expand: they count every candidate and report no
+// first insertions (emission happens after the expansion).
+struct CountMap {
+    uint32_t* keys;
+    uint32_t* vals;
+    uint32_t lg;
+    uint32_t* err;
+    __device__ __forceinline__ bool insert(uint32_t z, bool act) {
+        if (act) {
+            uint32_t s = smem_map_slot(keys, lg, z, err);
+            if (s != 0xFFFFFFFFu) atomicAdd(&vals[s], 1u);
+        }
+        return false;
+    }
+};
+struct CountTile {
+    uint32_t* ctr;
+    uint32_t lo;
+    __device__ __forceinline__ bool insert(uint32_t z, bool act) {
+        if (act) atomicAdd(&ctr[z - lo], 1u);
+        return false;
+    }
+};
+struct NullSink {
+    static constexpr bool kValues = false;
+    __device__ __forceinline__ void take(const uint32_t (&)[kUnroll], const uint32_t (&)[kUnroll]) {}
+};
+
 // Warp-collective emission of occupied map slots [s0, s1) with stride 32.
-// *pos is the row-local running slot (warp-uniform for class 1; for class 2
-// the caller passes a shared counter through `shared_pos`).
+// shared_pos: CTA-wide row-local slot counter; nullptr for a warp-owned row
+// (then *local_pos is the running slot).
 __device__ __forceinline__ void emit_map_slots_warp(const RowCtx& c, AggOut ao, const uint32_t* keys,
                                                     const uint32_t* vals, uint32_t s0, uint32_t s1, uint32_t xv,
                                                     unsigned long long base, uint32_t lim, uint32_t* shared_pos,
@@ -72,12 +100,12 @@ __device__ __forceinline__ void emit_map_slots_warp(const RowCtx& c, AggOut ao, 
 
 // Class 1 write pass: one warp per row; per warp 2^lg keys + 2^lg counts.
 __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
-                                                  const uint32_t* __restrict__ nrows_p, uint32_t warp_lg) {
+                                                  const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
     uint32_t* keys = smem + ((size_t)wib << (warp_lg + 1));
     uint32_t* vals = keys + (1u << warp_lg);
-    const uint32_t nrows = *nrows_p;
+    const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         const uint32_t x = rows[ri];
         uint32_t lg = ceil_log2(2 * c.ucap[x]);
@@ -87,13 +115,9 @@ __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uin
             vals[s] = 0;
         }
         __syncwarp();
-        auto ins = [&](uint32_t z) {
-            uint32_t s = smem_map_slot(keys, lg, z, c.err);
-            if (s != 0xFFFFFFFFu) atomicAdd(&vals[s], 1u);
-            return false;
-        };
-        auto emit = [&](bool, uint32_t) {};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 32, 0, c.T, ins, emit);
+        CountMap set{keys, vals, lg, c.err};
+        NullSink sink;
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
         __syncwarp();
         uint32_t pos = 0;
         emit_map_slots_warp(c, ao, keys, vals, 0, 1u << lg, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
@@ -103,14 +127,15 @@ __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uin
 
 // Class 2 write pass: one CTA per row.
 __global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
-                                                   const uint32_t* __restrict__ nrows_p, uint32_t block_lg) {
+                                                   const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
-    __shared__ uint32_t s_pos;
+    __shared__ uint32_t s_pos, s_row;
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(nw);
     uint32_t* keys = smem;
     uint32_t* vals = smem + (1u << block_lg);
-    const uint32_t nrows = *nrows_p;
-    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
         uint32_t lg = ceil_log2(2 * c.ucap[x]);
         lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
@@ -120,30 +145,27 @@ __global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const ui
         }
         if (threadIdx.x == 0) s_pos = 0;
         __syncthreads();
-        auto ins = [&](uint32_t z) {
-            uint32_t s = smem_map_slot(keys, lg, z, c.err);
-            if (s != 0xFFFFFFFFu) atomicAdd(&vals[s], 1u);
-            return false;
-        };
-        auto emit = [&](bool, uint32_t) {};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, 0, c.T, ins, emit);
+        CountMap set{keys, vals, lg, c.err};
+        NullSink sink;
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
         __syncthreads();
         const uint32_t span = (1u << lg);
         const uint32_t per = (span + nw - 1) / nw;
         const uint32_t s0 = min(span, wib * per), s1 = min(span, s0 + per);
         emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
-        __syncthreads();
     }
 }
 
-// Class 3 write pass: one CTA per row; a counter per z of one tile.
+// Classes 3/4 write pass: one CTA per row; a counter per z of one tile.
 __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
-                                                   const uint32_t* __restrict__ nrows_p) {
+                                                   const unsigned long long* __restrict__ n3,
+                                                   const unsigned long long* __restrict__ n4) {
     extern __shared__ uint32_t ctr[];
-    __shared__ uint32_t s_pos;
+    __shared__ uint32_t s_pos, s_row;
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t nrows = *nrows_p;
-    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+    const uint32_t nw_lg = 31 - __clz(nw);
+    const uint32_t nrows = (uint32_t)(*n3 + *n4);
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
         const uint32_t x = rows[ri];
         const unsigned long long base = c.off[x];
         const uint32_t lim = c.cnt[x], xv = c.id2x[x];
@@ -153,12 +175,9 @@ __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, const ui
             const uint32_t width = min(c.tile_width, c.m - lo);
             for (uint32_t w = threadIdx.x; w < width; w += blockDim.x) ctr[w] = 0;
             __syncthreads();
-            auto ins = [&](uint32_t z) {
-                atomicAdd(&ctr[z - lo], 1u);
-                return false;
-            };
-            auto emit = [&](bool, uint32_t) {};
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, t, t + 1, ins, emit);
+            CountTile set{ctr, lo};
+            NullSink sink;
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
             __syncthreads();
             // emit the nonzero counters of this tile
             for (uint32_t wb = wib * 32; wb < width; wb += nw * 32) {

@@ -80,8 +80,9 @@ constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counter
 
 struct Scalars {
     unsigned long long nx, ny, nz, nkept, total, outj;
-    unsigned long long nrows[4];
+    unsigned long long nrows[5];   // rows per class (index = class)
     unsigned int err;
+    unsigned int next_row[4];      // dynamic row counters of the CTA classes
     unsigned int pad;
 };
 
@@ -103,6 +104,7 @@ struct dim3g_ctx {
     size_t d_out_bytes = 0;
     Scalars* h_sc = nullptr;  // pinned
     cudaEvent_t ev[6] = {};
+    uint64_t launches = 0;  // kernels launched on this context since creation
 };
 
 struct dim3g_mapper {
@@ -131,7 +133,25 @@ int fail(dim3g_ctx* c, int code, const char* fmt, ...) {
         if (e_ != cudaSuccess) return fail(c, DIM3G_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
-#define CHECK_LAUNCH() CU(cudaGetLastError())
+#define CHECK_LAUNCH()         \
+    do {                       \
+        CU(cudaGetLastError());\
+        c->launches++;         \
+    } while (0)
+
+// device_scan plus launch accounting (three kernels when n > 0).
+template <class Src, class Dst>
+int run_scan(dim3g_ctx* c, Src src, Dst dst, uint64_t n, uint64_t* bsum, unsigned long long* total) {
+    device_scan(src, dst, n, bsum, total, c->stream);
+    CU(cudaGetLastError());
+    c->launches += n ? 3 : 0;
+    return DIM3G_OK;
+}
+#define SCAN(...)                                \
+    do {                                         \
+        int r_ = run_scan(c, __VA_ARGS__);       \
+        if (r_) return r_;                       \
+    } while (0)
 
 uint64_t next_pow2(uint64_t v) {
     uint64_t p = 1;
@@ -172,8 +192,22 @@ struct JoinPlan {
 };
 
 bool set_aggregate_attributes();
-int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const uint32_t* list_w, const uint32_t* list_b,
-                        const uint32_t* list_m, const uint32_t* nr_w, const uint32_t* nr_b, const uint32_t* nr_m);
+struct RowLists {
+    const uint32_t *w, *b, *m;                          // class 1, class 2, classes 4 then 3
+    const unsigned long long *nw, *nb, *n3, *n4;        // their sizes (device)
+};
+int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const RowLists& L);
+
+// Grid of a persistent / grid-stride kernel: resident CTAs per SM x SMs.
+template <class K>
+unsigned resident_grid(K kernel, int block, size_t smem, int sm) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        per = 1;
+    }
+    return (unsigned)(per * sm);
+}
 
 int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     cudaStream_t st = c->stream;
@@ -211,11 +245,11 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
 
     k_insert_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, &sc->err);
     CHECK_LAUNCH();
-    device_scan(OccupiedSrc{ty.slots}, AssignIdDst{ty.slots, nullptr}, capP, bsum, &sc->ny, st);
-    device_scan(OccupiedSrc{tx.slots}, AssignIdDst{tx.slots, id2x}, capP, bsum, &sc->nx, st);
+    SCAN(OccupiedSrc{ty.slots}, AssignIdDst{ty.slots, nullptr}, capP, bsum, &sc->ny);
+    SCAN(OccupiedSrc{tx.slots}, AssignIdDst{tx.slots, id2x}, capP, bsum, &sc->nx);
     k_probe_q<<<grid_for(jp.nQ, sm), 256, 0, st>>>(jp.Q, jp.nQ, ty, tz, Qk, &sc->nkept, &sc->err);
     CHECK_LAUNCH();
-    device_scan(OccupiedSrc{tz.slots}, AssignIdDst{tz.slots, id2z}, capQ, bsum, &sc->nz, st);
+    SCAN(OccupiedSrc{tz.slots}, AssignIdDst{tz.slots, id2z}, capQ, bsum, &sc->nz);
     CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in mapping (flags %u)", c->h_sc->err);
@@ -254,13 +288,15 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cur_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* JR_S = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* IC_S = ws_get<uint32_t>(c, nq);
+    uint32_t* VS = ws_get<uint32_t>(c, nq);
+    uint32_t* Zq = ws_get<uint32_t>(c, nq);
     uint32_t* ucap = ws_get<uint32_t>(c, n);
     uint8_t* cls = ws_get<uint8_t>(c, n);
     uint32_t* lists = ws_get<uint32_t>(c, (uint64_t)3 * n);
-    uint32_t* cnt = ws_get<uint32_t>(c, n);
+    uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
     uint64_t* bsum2 = ws_get<uint64_t>(c, scan_blocks((nyt > n ? nyt : n) + 1) + 1);
-    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !ucap || !cls || !lists ||
+    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !VS || !Zq || !ucap || !cls || !lists ||
         !cnt || !off || !bsum2)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
 
@@ -268,13 +304,13 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     CU(cudaMemsetAsync(cnt_yt, 0, (nyt + 1) * 4, st));
     k_map_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, Pm, degx);
     CHECK_LAUNCH();
-    k_map_q<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, tz, T, tile_shift, cnt_yt);
+    k_map_q<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, tz, T, tile_shift, Zq, cnt_yt);
     CHECK_LAUNCH();
-    device_scan(U32Src{degx}, RowPtrDst{JR_R, curx}, (uint64_t)n + 1, bsum2, nullptr, st);
+    SCAN(U32Src{degx}, RowPtrDst{JR_R, curx}, (uint64_t)n + 1, bsum2, nullptr);
     k_scatter_r<<<grid_for(jp.nP, sm), 256, 0, st>>>(Pm, jp.nP, curx, IC_R);
     CHECK_LAUNCH();
-    device_scan(U32Src{cnt_yt}, RowPtrDst{JR_S, cur_yt}, nyt + 1, bsum2, nullptr, st);
-    k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, T, tile_shift, cur_yt, IC_S);
+    SCAN(U32Src{cnt_yt}, RowPtrDst{JR_S, cur_yt}, nyt + 1, bsum2, nullptr);
+    k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, Zq, nq, T, tile_shift, cur_yt, IC_S, VS);
     CHECK_LAUNCH();
 
     RowCtx rc{};
@@ -282,6 +318,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     rc.IC_R = IC_R;
     rc.JR_S = JR_S;
     rc.IC_S = IC_S;
+    rc.VS = VS;
     rc.T = T;
     rc.tile_width = tile_width;
     rc.m = m;
@@ -300,28 +337,34 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* list_w = lists;
     uint32_t* list_b = lists + n;
     uint32_t* list_m = lists + 2 * (uint64_t)n;
-    device_scan(ClassSrc{cls, 1}, ListDst{list_w}, n, bsum2, &sc->nrows[1], st);
-    device_scan(ClassSrc{cls, 2}, ListDst{list_b}, n, bsum2, &sc->nrows[2], st);
-    device_scan(ClassSrc{cls, 3}, ListDst{list_m}, n, bsum2, &sc->nrows[3], st);
-    CU(cudaMemsetAsync(cnt, 0, (uint64_t)n * 4, st));
+    SCAN(ClassSrc{cls, 1}, ListDst{list_w, nullptr}, n, bsum2, &sc->nrows[1]);
+    SCAN(ClassSrc{cls, 2}, ListDst{list_b, nullptr}, n, bsum2, &sc->nrows[2]);
+    // bitmap rows: class 4 (huge) first, then class 3
+    SCAN(ClassSrc{cls, 4}, ListDst{list_m, nullptr}, n, bsum2, &sc->nrows[4]);
+    SCAN(ClassSrc{cls, 3}, ListDst{list_m, &sc->nrows[4]}, n, bsum2, &sc->nrows[3]);
+    CU(cudaMemsetAsync(cnt, 0, ((uint64_t)n + 1) * 4, st));
     CU(cudaEventRecord(c->ev[2], st));
 
-    // nrows are read on the device; the grids are fixed multiples of the SMs
-    const uint32_t* nr_w = (const uint32_t*)&sc->nrows[1];
-    const uint32_t* nr_b = (const uint32_t*)&sc->nrows[2];
-    const uint32_t* nr_m = (const uint32_t*)&sc->nrows[3];
+    // Row counts are read on the device; grids are resident CTAs x SMs.
+    const RowLists L{list_w, list_b, list_m, &sc->nrows[1], &sc->nrows[2], &sc->nrows[3], &sc->nrows[4]};
+    rc.next_row = sc->next_row;
     const size_t smem_w = (size_t)8 << c->prm.warp_lg << 2;
     const size_t smem_b = (size_t)1 << c->prm.block_lg << 2;
-    const size_t smem_m = (size_t)((tile_width + 31) / 32) * 4;
-    const unsigned g_w = (unsigned)sm * 4, g_b = (unsigned)sm * 3, g_m = (unsigned)sm * 2;
+    size_t smem_m = (size_t)((((tile_width + 31) / 32) + 3) / 4) * 16;  // whole uint4 words (cleared as uint4)
+    if (smem_m < 128) smem_m = 128;  // idle lanes touch words 0..31
+    const int blk_m = tile_width > (1u << 19) ? 1024 : 512;
+    const unsigned g_w = resident_grid(k_rows_warp<true>, 256, smem_w, sm);
+    const unsigned g_b = resident_grid(k_rows_block<true>, 256, smem_b, sm);
+    const unsigned g_m = resident_grid(k_rows_bitmap<true>, blk_m, smem_m, sm);
 
-    k_rows_warp<false><<<g_w, 256, smem_w, st>>>(rc, list_w, nr_w, c->prm.warp_lg);
+    // count pass (the bitmap rows, the largest, start first)
+    k_rows_bitmap<false><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
-    k_rows_block<false><<<g_b, 256, smem_b, st>>>(rc, list_b, nr_b, c->prm.block_lg);
+    k_rows_block<false><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
     CHECK_LAUNCH();
-    k_rows_bitmap<false><<<g_m, 512, smem_m, st>>>(rc, list_m, nr_m);
+    k_rows_warp<false><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
     CHECK_LAUNCH();
-    device_scan(U32Src{cnt}, OffDst{off}, (uint64_t)n + 1, bsum2, &sc->total, st);
+    SCAN(U32Src{cnt}, OffDst{off}, (uint64_t)n + 1, bsum2, &sc->total);
     CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     CU(cudaEventRecord(c->ev[3], st));
     CU(cudaStreamSynchronize(st));
@@ -331,7 +374,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     S.n_out = total;
     S.rows_warp = (uint32_t)c->h_sc->nrows[1];
     S.rows_block = (uint32_t)c->h_sc->nrows[2];
-    S.rows_bitmap = (uint32_t)c->h_sc->nrows[3];
+    S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
     *n_out = total;
     if (jp.count_only) {
         float a, b, d;
@@ -349,16 +392,17 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     int pr = jp.prep.fn(c, jp.prep.user, total, &out, &out_cnt);
     if (pr) return pr;
     rc.out = out;
+    CU(cudaMemsetAsync(sc->next_row, 0, sizeof(sc->next_row), st));
     if (total > 0) {
         if (jp.aggregate) {
-            int r = run_aggregate_write(c, rc, AggOut{out_cnt}, list_w, list_b, list_m, nr_w, nr_b, nr_m);
+            int r = run_aggregate_write(c, rc, AggOut{out_cnt}, L);
             if (r) return r;
         } else {
-            k_rows_warp<true><<<g_w, 256, smem_w, st>>>(rc, list_w, nr_w, c->prm.warp_lg);
+            k_rows_bitmap<true><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
             CHECK_LAUNCH();
-            k_rows_block<true><<<g_b, 256, smem_b, st>>>(rc, list_b, nr_b, c->prm.block_lg);
+            k_rows_block<true><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
             CHECK_LAUNCH();
-            k_rows_bitmap<true><<<g_m, 512, smem_m, st>>>(rc, list_m, nr_m);
+            k_rows_warp<true><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
             CHECK_LAUNCH();
         }
     }
@@ -379,18 +423,17 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     return DIM3G_OK;
 }
 
-int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const uint32_t* list_w, const uint32_t* list_b,
-                        const uint32_t* list_m, const uint32_t* nr_w, const uint32_t* nr_b, const uint32_t* nr_m) {
+int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const RowLists& L) {
     cudaStream_t st = c->stream;
     const int sm = c->sm_count;
     const size_t smem_w = (size_t)8 << (c->prm.warp_lg + 1) << 2;
     const size_t smem_b = (size_t)2 << c->prm.block_lg << 2;
     const size_t smem_m = (size_t)rc.tile_width * 4;
-    k_agg_warp<<<(unsigned)sm * 2, 256, smem_w, st>>>(rc, ao, list_w, nr_w, c->prm.warp_lg);
+    k_agg_tile<<<resident_grid(k_agg_tile, 1024, smem_m, sm), 1024, smem_m, st>>>(rc, ao, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
-    k_agg_block<<<(unsigned)sm * 2, 256, smem_b, st>>>(rc, ao, list_b, nr_b, c->prm.block_lg);
+    k_agg_block<<<resident_grid(k_agg_block, 256, smem_b, sm), 256, smem_b, st>>>(rc, ao, L.b, L.nb, c->prm.block_lg);
     CHECK_LAUNCH();
-    k_agg_tile<<<(unsigned)sm, 1024, smem_m, st>>>(rc, ao, list_m, nr_m);
+    k_agg_warp<<<resident_grid(k_agg_warp, 256, smem_w, sm), 256, smem_w, st>>>(rc, ao, L.w, L.nw, c->prm.warp_lg);
     CHECK_LAUNCH();
     return DIM3G_OK;
 }
@@ -577,6 +620,7 @@ const char* dim3g_last_error(const dim3g_ctx* c) { return c ? c->err.c_str() : "
 int dim3g_get_stats(const dim3g_ctx* c, dim3g_stats* out) {
     if (!c || !out) return DIM3G_ERR_INVALID;
     *out = c->stats;
+    out->launches = c->launches;
     return DIM3G_OK;
 }
 
@@ -769,7 +813,7 @@ int dim3g_mapper_insert(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32
     CU(cudaMemsetAsync(err, 0, 4, st));
     k_mapper_claim<<<grid_for(n, c->sm_count), 256, 0, st>>>(t, dk, n, err);
     CHECK_LAUNCH();
-    device_scan(FirstOccSrc{t, dk}, AssignNewIdDst{t, dk, (long long)m->cnt}, n, bsum, total, st);
+    SCAN(FirstOccSrc{t, dk}, AssignNewIdDst{t, dk, (long long)m->cnt}, n, bsum, total);
     k_mapper_gather<<<grid_for(n, c->sm_count), 256, 0, st>>>(t, dk, n, di);
     CHECK_LAUNCH();
     unsigned long long h_total = 0;

@@ -4,26 +4,30 @@
 // For an x row the candidates are every z of S row y for every y of R row x.
 // Rows are binned by u = min(candidates, m), an upper bound on their distinct
 // outputs:
-//   class 1 (u <= cap_w): one warp per row, a private shared-memory hash set
-//   class 2 (u <= cap_b): one CTA per row, a shared-memory hash set
-//   class 3 (u >  cap_b): one CTA per row, a shared-memory bitmap over one
-//                          z tile at a time (S is bucketed by (y, z tile)).
-// Each kernel runs twice: a count pass writes cnt[x] = |distinct z|; after a
-// prefix sum over cnt the write pass repeats the expansion and every first
-// insertion of a z emits (x value, z value) at off[x] + a row-local slot, so
-// each row's pairs are contiguous and the whole output is dense.
+//   class 1 (u <= cap_w):  one warp per row, a private shared-memory hash set
+//   class 2 (u <= cap_b):  one CTA per row, a shared-memory hash set
+//   class 3/4 (u > cap_b): one CTA per row, a shared-memory bitmap over one
+//                          z tile at a time (S is bucketed by (y, z tile));
+//                          class 4 (u > kHugeRow) rows are scheduled first.
+// CTA classes take rows dynamically from an atomic counter.  Each kernel
+// runs twice: a count pass writes cnt[x] = |distinct z|; after a prefix sum
+// over cnt the write pass repeats the expansion and every first insertion of
+// a z emits (x value, z value) at off[x] + a row-local slot, so each row's
+// pairs are contiguous and the whole output is dense.
 #pragma once
 #include "common.cuh"
 
 namespace dim3g {
 
 constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
+constexpr uint32_t kHugeRow = 1u << 16;
 
 struct RowCtx {
     const uint32_t* JR_R;  // n+1 row pointers of R by x id
     const uint32_t* IC_R;  // y ids
     const uint32_t* JR_S;  // k*T+1 row pointers of S by (y id, z tile)
     const uint32_t* IC_S;  // z ids
+    const uint32_t* VS;    // z values, parallel to IC_S (write pass)
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
@@ -34,6 +38,7 @@ struct RowCtx {
     const uint32_t* id2z;
     uint2* out;
     uint32_t* err;
+    uint32_t* next_row;    // dynamic row counters of the CTA classes
 };
 
 __device__ __forceinline__ uint32_t ceil_log2(uint32_t v) { return v <= 1 ? 0 : 32 - __clz(v - 1); }
@@ -58,84 +63,179 @@ __device__ __forceinline__ bool smem_set_insert(uint32_t* tab, uint32_t lg, uint
     return false;
 }
 
-// Warp-cooperative expansion of R entries [e0, e1) over S tiles [t0, t1).
-// The warp takes chunks of 32 entries starting at e0 + chunk0, stepping by
-// chunk_step; within a chunk the candidate space is flattened by a warp
-// prefix sum over segment lengths and every lane locates its segment by a
-// 5-step binary search over the lanes' inclusive prefixes, so lanes stay
-// busy whatever the segment lengths.  ins(z) -> bool runs per lane;
-// emit(isnew, z) is warp-collective.
-template <class Ins, class Emit>
-__device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t chunk0,
-                                            uint32_t chunk_step, uint32_t t0, uint32_t t1, Ins& ins, Emit& emit) {
+#ifndef DIM3G_UNROLL
+#define DIM3G_UNROLL 4
+#endif
+#ifndef DIM3G_MIN_PIECE
+#define DIM3G_MIN_PIECE 256
+#endif
+constexpr uint32_t kUnroll = DIM3G_UNROLL;
+constexpr uint32_t kMinPiece = DIM3G_MIN_PIECE;
+
+// Warp-level expansion of the candidates of R entries [e0, e1) over S tiles
+// [t0, t1).  Entries are taken 32 at a time; a warp prefix sum over their S
+// segment lengths flattens the chunk's candidates into [0, total), which is
+// cut into a power-of-two number (<= nparts) of contiguous pieces of at least
+// kMinPiece candidates; the calling warp takes piece `part`.  It finds the
+// segment holding its first candidate with one ballot over the lanes'
+// inclusive prefixes, then walks the segments overlapping its piece, the
+// lanes striding each segment kUnroll x 32 candidates at a time.
+//   set.insert(z, active) -> bool   per lane (false when !active)
+//   sink.take(b[], v[])             warp-collective once per group: b[u] is
+//                                   the ballot of first insertions of step u;
+//                                   v[u] is the lane's z value when the sink
+//                                   asks for values (Sink::kValues), loaded
+//                                   together with the z id to hide latency
+template <class Set, class Sink>
+__device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t part,
+                                            uint32_t nparts_lg, uint32_t t0, uint32_t t1, Set& set, Sink& sink) {
     const uint32_t lane = lane_id();
-    for (uint32_t eb = e0 + chunk0; eb < e1; eb += chunk_step) {
-        uint32_t e = eb + lane;
+    for (uint32_t eb = e0; eb < e1; eb += 32) {
+        const uint32_t e = eb + lane;
         uint32_t s0 = 0, len = 0;
         if (e < e1) {
-            uint32_t y = __ldg(&c.IC_R[e]);
-            uint64_t r = (uint64_t)y * c.T;
+            const uint32_t y = __ldg(&c.IC_R[e]);
+            const uint64_t r = (uint64_t)y * c.T;
             s0 = __ldg(&c.JR_S[r + t0]);
             len = __ldg(&c.JR_S[r + t1]) - s0;
         }
-        uint32_t incl = warp_incl_scan(len);
-        uint32_t excl = incl - len;
-        uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        for (uint32_t base = 0; base < total; base += 32) {
-            uint32_t ci = base + lane;
-            int lo = 0;
+        const uint32_t incl = warp_incl_scan(len);
+        if (__any_sync(0xffffffffu, incl < len)) raise_error(c.err, kErrCountRange);
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t want = total / kMinPiece;
+        uint32_t np_lg = want <= 1 ? 0 : 31 - __clz(want);
+        np_lg = np_lg > nparts_lg ? nparts_lg : np_lg;
+        if (part >= (1u << np_lg)) continue;
+        const uint32_t piece = (total >> np_lg) + ((total & ((1u << np_lg) - 1)) ? 1u : 0u);
+        const uint32_t p0 = min(part * piece, total);
+        const uint32_t p1 = min(p0 + piece, total);
+        if (p0 >= p1) continue;
+        const uint32_t excl = incl - len;
+        // first segment holding candidate p0: lanes with incl <= p0 form a prefix
+        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, incl <= p0)); k < 32; k++) {
+            const uint32_t kex = __shfl_sync(0xffffffffu, excl, k);
+            if (kex >= p1) break;
+            const uint32_t klen = __shfl_sync(0xffffffffu, len, k);
+            const uint32_t ks0 = __shfl_sync(0xffffffffu, s0, k);
+            const uint32_t lo = (p0 > kex ? p0 - kex : 0);
+            const uint32_t hi = (kex + klen < p1 ? klen : p1 - kex);
+            for (uint32_t jb = lo; jb < hi; jb += 32 * kUnroll) {
+                uint32_t z[kUnroll], v[kUnroll];
 #pragma unroll
-            for (int step = 16; step >= 1; step >>= 1) {
-                uint32_t v = __shfl_sync(0xffffffffu, incl, lo + step - 1);
-                if (v <= ci) lo += step;
+                for (uint32_t u = 0; u < kUnroll; u++) {
+                    const uint32_t j = jb + u * 32 + lane;
+                    z[u] = j < hi ? __ldg(&c.IC_S[ks0 + j]) : kEmpty32;
+                    if (Sink::kValues) v[u] = j < hi ? __ldg(&c.VS[ks0 + j]) : 0u;
+                }
+                uint32_t b[kUnroll];
+#pragma unroll
+                for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32));
+                sink.take(b, v);
             }
-            uint32_t ks0 = __shfl_sync(0xffffffffu, s0, lo);
-            uint32_t kex = __shfl_sync(0xffffffffu, excl, lo);
-            bool isnew = false;
-            uint32_t z = 0;
-            if (ci < total) {
-                z = __ldg(&c.IC_S[ks0 + (ci - kex)]);
-                isnew = ins(z);
-            }
-            emit(isnew, z);
         }
     }
+}
+
+// ----------------------------------------------------------------- sets
+struct HashSet {
+    uint32_t* tab;
+    uint32_t lg;
+    uint32_t* err;
+    __device__ __forceinline__ bool insert(uint32_t z, bool act) { return act ? smem_set_insert(tab, lg, z, err) : false; }
+};
+
+// Bitmap over one z tile; branch-free (idle lanes OR a zero into words
+// 0..31, so the bitmap allocation is at least 32 words).
+struct TileBitmap {
+    uint32_t* bm;
+    uint32_t lo;
+    __device__ __forceinline__ bool insert(uint32_t z, bool act) {
+        const uint32_t zl = z - lo;
+        const uint32_t w = act ? (zl >> 5) : lane_id();
+        const uint32_t bit = act ? (1u << (zl & 31)) : 0u;
+        return (atomicOr(&bm[w], bit) & bit) == 0 && act;
+    }
+};
+
+// ---------------------------------------------------------------- sinks
+struct CountSink {
+    static constexpr bool kValues = false;
+    uint32_t count = 0;
+    __device__ __forceinline__ void take(const uint32_t (&b)[kUnroll], const uint32_t (&)[kUnroll]) {
+#pragma unroll
+        for (uint32_t u = 0; u < kUnroll; u++) count += __popc(b[u]);
+    }
+};
+
+// Emits first insertions at base + a row-local slot.  shared_pos == nullptr:
+// the warp owns the row and counts locally; otherwise one shared-memory claim
+// per group reserves the slots.
+struct WriteSink {
+    static constexpr bool kValues = true;
+    uint2* out;
+    uint32_t* err;
+    unsigned long long base;
+    uint32_t lim, xv;
+    uint32_t* shared_pos;
+    uint32_t local = 0;
+    __device__ __forceinline__ void take(const uint32_t (&b)[kUnroll], const uint32_t (&v)[kUnroll]) {
+        uint32_t n = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < kUnroll; u++) n += __popc(b[u]);
+        if (n == 0) return;
+        uint32_t pb;
+        if (shared_pos) {
+            pb = 0;
+            if (lane_id() == 0) pb = atomicAdd(shared_pos, n);
+            pb = __shfl_sync(0xffffffffu, pb, 0);
+        } else {
+            pb = local;
+            local += n;
+        }
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (uint32_t u = 0; u < kUnroll; u++) {
+            if (b[u] & (1u << lane_id())) {
+                const uint32_t pos = pb + __popc(b[u] & lt);
+                if (pos < lim) out[base + pos] = make_uint2(xv, v[u]);
+                else raise_error(err, kErrOutputBound);
+            }
+            pb += __popc(b[u]);
+        }
+    }
+};
+
+// Next row of a CTA class, taken dynamically (the whole CTA gets the index).
+__device__ __forceinline__ uint32_t cta_next_row(uint32_t* counter, uint32_t* s_row) {
+    __syncthreads();
+    if (threadIdx.x == 0) *s_row = atomicAdd(counter, 1u);
+    __syncthreads();
+    return *s_row;
 }
 
 // Class 1: one warp per row, 2^warp_lg slots per warp.
 template <bool WRITE>
 __global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __restrict__ rows,
-                                                   const uint32_t* __restrict__ nrows_p, uint32_t warp_lg) {
+                                                   const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
     uint32_t* tab = smem + ((size_t)wib << warp_lg);
-    const uint32_t nrows = *nrows_p;
+    const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         const uint32_t x = rows[ri];
         uint32_t lg = ceil_log2(2 * c.ucap[x]);
         lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
         for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
         __syncwarp();
-        uint32_t count = 0;
-        unsigned long long base = 0;
-        uint32_t lim = 0, xv = 0;
+        HashSet set{tab, lg, c.err};
         if (WRITE) {
-            base = c.off[x];
-            lim = c.cnt[x];
-            xv = c.id2x[x];
+            WriteSink sink{c.out, c.err, c.off[x], c.cnt[x], c.id2x[x], nullptr};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+        } else {
+            CountSink sink;
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+            if (lane == 0) c.cnt[x] = sink.count;
         }
-        auto ins = [&](uint32_t z) { return smem_set_insert(tab, lg, z, c.err); };
-        auto emit = [&](bool isnew, uint32_t z) {
-            uint32_t b = __ballot_sync(0xffffffffu, isnew);
-            if (WRITE && isnew) {
-                uint32_t pos = count + __popc(b & lanemask_lt());
-                if (pos < lim) c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[z]));
-                else raise_error(c.err, kErrOutputBound);
-            }
-            count += __popc(b);
-        };
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 32, 0, c.T, ins, emit);
-        if (!WRITE && lane == 0) c.cnt[x] = count;
         __syncwarp();
     }
 }
@@ -143,107 +243,80 @@ __global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __r
 // Class 2: one CTA per row, 2^block_lg slots.
 template <bool WRITE>
 __global__ void __launch_bounds__(256) k_rows_block(RowCtx c, const uint32_t* __restrict__ rows,
-                                                    const uint32_t* __restrict__ nrows_p, uint32_t block_lg) {
+                                                    const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
-    __shared__ uint32_t s_count;
-    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t nrows = *nrows_p;
-    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+    __shared__ uint32_t s_count, s_row;
+    const uint32_t wib = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
         uint32_t lg = ceil_log2(2 * c.ucap[x]);
         lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
-        for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) smem[s] = kEmpty32;
+        uint4* t4 = reinterpret_cast<uint4*>(smem);
+        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
+            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
         if (threadIdx.x == 0) s_count = 0;
         __syncthreads();
-        unsigned long long base = 0;
-        uint32_t lim = 0, xv = 0, wcount = 0;
+        HashSet set{smem, lg, c.err};
         if (WRITE) {
-            base = c.off[x];
-            lim = c.cnt[x];
-            xv = c.id2x[x];
+            WriteSink sink{c.out, c.err, c.off[x], c.cnt[x], c.id2x[x], &s_count};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        } else {
+            CountSink sink;
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+            if (lane == 0 && sink.count) atomicAdd(&s_count, sink.count);
         }
-        auto ins = [&](uint32_t z) { return smem_set_insert(smem, lg, z, c.err); };
-        auto emit = [&](bool isnew, uint32_t z) {
-            uint32_t b = __ballot_sync(0xffffffffu, isnew);
-            if (WRITE) {
-                uint32_t pb = 0;
-                if (lane == 0 && b) pb = atomicAdd(&s_count, (uint32_t)__popc(b));
-                pb = __shfl_sync(0xffffffffu, pb, 0);
-                if (isnew) {
-                    uint32_t pos = pb + __popc(b & lanemask_lt());
-                    if (pos < lim) c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[z]));
-                    else raise_error(c.err, kErrOutputBound);
-                }
-            } else {
-                wcount += __popc(b);
-            }
-        };
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, 0, c.T, ins, emit);
-        if (!WRITE && lane == 0 && wcount) atomicAdd(&s_count, wcount);
         __syncthreads();
         if (!WRITE && threadIdx.x == 0) c.cnt[x] = s_count;
-        __syncthreads();
     }
 }
 
-// Class 3: one CTA per row, a bitmap over one z tile at a time.
+// Classes 3 and 4: one CTA per row, a bitmap over one z tile at a time.  The
+// row list holds the class-4 rows first; nrows = *n4 + *n3.
 template <bool WRITE>
-__global__ void __launch_bounds__(512) k_rows_bitmap(RowCtx c, const uint32_t* __restrict__ rows,
-                                                     const uint32_t* __restrict__ nrows_p) {
+__global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uint32_t* __restrict__ rows,
+                                                      const unsigned long long* __restrict__ n3,
+                                                      const unsigned long long* __restrict__ n4) {
     extern __shared__ uint32_t bm[];
-    __shared__ uint32_t s_count;
-    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    const uint32_t nrows = *nrows_p;
-    for (uint32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+    __shared__ uint32_t s_count, s_row;
+    const uint32_t wib = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    const uint32_t nrows = (uint32_t)(*n3 + *n4);
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
         const uint32_t x = rows[ri];
         if (threadIdx.x == 0) s_count = 0;
-        unsigned long long base = 0;
-        uint32_t lim = 0, xv = 0, wcount = 0;
+        WriteSink wsink{c.out, c.err, 0, 0, 0, &s_count};
         if (WRITE) {
-            base = c.off[x];
-            lim = c.cnt[x];
-            xv = c.id2x[x];
+            wsink.base = c.off[x];
+            wsink.lim = c.cnt[x];
+            wsink.xv = c.id2x[x];
         }
+        CountSink csink;
         for (uint32_t t = 0; t < c.T; t++) {
             const uint32_t lo = t * c.tile_width;
             const uint32_t width = min(c.tile_width, c.m - lo);
-            const uint32_t words = (width + 31) >> 5;
-            for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bm[w] = 0;
+            const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
+            uint4* b4 = reinterpret_cast<uint4*>(bm);
+            for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
             __syncthreads();
-            auto ins = [&](uint32_t z) {
-                uint32_t zl = z - lo, bit = 1u << (zl & 31);
-                uint32_t old = atomicOr(&bm[zl >> 5], bit);
-                return (old & bit) == 0;
-            };
-            auto emit = [&](bool isnew, uint32_t z) {
-                uint32_t b = __ballot_sync(0xffffffffu, isnew);
-                if (WRITE) {
-                    uint32_t pb = 0;
-                    if (lane == 0 && b) pb = atomicAdd(&s_count, (uint32_t)__popc(b));
-                    pb = __shfl_sync(0xffffffffu, pb, 0);
-                    if (isnew) {
-                        uint32_t pos = pb + __popc(b & lanemask_lt());
-                        if (pos < lim) c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[z]));
-                        else raise_error(c.err, kErrOutputBound);
-                    }
-                } else {
-                    wcount += __popc(b);
-                }
-            };
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib * 32, nw * 32, t, t + 1, ins, emit);
+            TileBitmap set{bm, lo};
+            if (WRITE) warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, wsink);
+            else warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, csink);
             __syncthreads();
         }
-        if (!WRITE && lane == 0 && wcount) atomicAdd(&s_count, wcount);
-        __syncthreads();
-        if (!WRITE && threadIdx.x == 0) c.cnt[x] = s_count;
-        __syncthreads();
+        if (!WRITE) {
+            if (lane == 0 && csink.count) atomicAdd(&s_count, csink.count);
+            __syncthreads();
+            if (threadIdx.x == 0) c.cnt[x] = s_count;
+        }
     }
 }
 
 // Per-row candidate count w = sum over y in R_x of |S_y|, u = min(w, m) and
-// the row class (0: empty).  One warp per row.
-// With check_range set (join-aggregate, 32-bit per-group counters) a row of
-// 2^32 or more candidates raises kErrCountRange.
+// the row class (0: empty).  One warp per row.  With check_range set
+// (join-aggregate, 32-bit per-group counters) a row of 2^32 or more
+// candidates raises kErrCountRange.
 __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range,
                            uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj) {
     const uint32_t lane = lane_id();
@@ -261,7 +334,7 @@ __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b,
         if (lane == 0) {
             uint32_t u = (uint32_t)(w < c.m ? w : c.m);
             ucap[x] = u;
-            cls[x] = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : 3));
+            cls[x] = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
             if (check_range && w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
             acc += w;
         }
@@ -274,10 +347,12 @@ struct ClassSrc {
     uint8_t want;
     __device__ uint64_t operator()(uint64_t i) const { return cls[i] == want ? 1u : 0u; }
 };
+// list[*base + rank] = row (base: count of rows placed before this class).
 struct ListDst {
     uint32_t* list;
+    const unsigned long long* base;
     __device__ void operator()(uint64_t i, uint64_t e, uint64_t v) const {
-        if (v) list[e] = (uint32_t)i;
+        if (v) list[(base ? *base : 0) + e] = (uint32_t)i;
     }
 };
 struct OffDst {

@@ -114,13 +114,14 @@ __global__ void k_map_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, De
     }
 }
 
-// Q' -> (z id, y id); histogram over the (y, z tile) CSR key y*T + z/TB.
-__global__ void k_map_q(uint2* __restrict__ Qk, uint64_t n, DevTable tz, uint32_t T, uint32_t tile_shift,
-                        uint32_t* __restrict__ cnt_yt) {
+// Q' = (z value, y id) -> z id; histogram over the (y, z tile) CSR key
+// y*T + z/TB.
+__global__ void k_map_q(const uint2* __restrict__ Qk, uint64_t n, DevTable tz, uint32_t T, uint32_t tile_shift,
+                        uint32_t* __restrict__ zid, uint32_t* __restrict__ cnt_yt) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 q = Qk[i];
         uint32_t zi = table_find(tz, q.x);
-        Qk[i] = make_uint2(zi, q.y);
+        zid[i] = zi;
         atomicAdd(&cnt_yt[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
     }
 }
@@ -148,12 +149,17 @@ __global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uint32_t* 
     }
 }
 
-__global__ void k_scatter_s(const uint2* __restrict__ Qm, uint64_t n, uint32_t T, uint32_t tile_shift,
-                            uint32_t* __restrict__ cursor, uint32_t* __restrict__ ic) {
+// S CSR by (y id, z tile): z ids into ic and, beside them, z values into vs
+// (the write pass emits values without a gather through id2z).
+__global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t* __restrict__ zid, uint64_t n, uint32_t T,
+                            uint32_t tile_shift, uint32_t* __restrict__ cursor, uint32_t* __restrict__ ic,
+                            uint32_t* __restrict__ vs) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint2 q = Qm[i];
-        uint32_t pos = atomicAdd(&cursor[(uint64_t)q.y * T + (q.x >> tile_shift)], 1u);
-        ic[pos] = q.x;
+        uint2 q = Qk[i];
+        uint32_t zi = zid[i];
+        uint32_t pos = atomicAdd(&cursor[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
+        ic[pos] = zi;
+        vs[pos] = q.x;
     }
 }
 

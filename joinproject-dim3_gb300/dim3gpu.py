@@ -17,7 +17,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libdim3gpu.so")
+# DIM3G_LIB selects an alternative build of the same library (tuning sweeps).
+LIB_PATH = os.environ.get("DIM3G_LIB") or os.path.join(HERE, "libdim3gpu.so")
 GEN_PATH = os.path.join(HERE, "libdim3gen.so")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_DEVICE, ERR_UNSUPPORTED = range(7)
@@ -42,7 +43,7 @@ class Stats(ctypes.Structure):
         ("rows_warp", ctypes.c_uint32), ("rows_block", ctypes.c_uint32), ("rows_bitmap", ctypes.c_uint32),
         ("rows_dense", ctypes.c_uint32), ("z_tiles", ctypes.c_uint32), ("heavy_y", ctypes.c_uint32),
         ("ms_map", ctypes.c_float), ("ms_csr", ctypes.c_float), ("ms_count", ctypes.c_float),
-        ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float),
+        ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float), ("launches", ctypes.c_uint64),
     ]
 
     def as_dict(self):
