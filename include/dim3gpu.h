@@ -9,9 +9,10 @@
  *   R = (x, y) pairs, S = (z, y) pairs.
  * The result is the distinct set {(P.first, Q.first) | P.y == Q.y} where P is
  * the larger input -- R when |R| >= |S|, otherwise S, exactly the reference's
- * swap (dim3.hpp:993-994), so a smaller R yields (z, x) pairs.  Pairs are
- * grouped by their first value; the order of groups and of pairs inside a
- * group is unspecified (the reference's order is unspecified too).
+ * swap (dim3.hpp:993-994), so a smaller R yields (z, x) pairs.  The order of
+ * the pairs is unspecified (the reference's order is an artifact of its id
+ * assignment too); with the "ordered_output" knob set, pairs come grouped by
+ * their first value, groups in a fixed order.
  *
  * Limits: |R|, |S| < 2^32 - 1 tuples; the distinct key domains below 2^31;
  * output counts are 64-bit (no wrap at 2^31, unlike myvector's uint32 count).
@@ -54,6 +55,8 @@ typedef struct {
     float ms_write;            /* device ms: write pass */
     float ms_total;            /* device ms: whole call (inputs resident) */
     uint64_t launches;         /* kernels launched on this context since creation */
+    float ms_count_cls[3];     /* count pass device ms per row kernel: bitmap, block, warp */
+    float ms_write_cls[3];     /* write pass device ms per row kernel: bitmap, block, warp */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */
@@ -67,7 +70,9 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
 /* Tuning knobs, validated on set: "warp_slots_log2" (5..11, warp-class hash
  * set size), "block_slots_log2" (8..14, block-class hash set size),
  * "tile_bits_log2" (10..20, bitmap-class z tile width), "heavy_min_len"
- * (minimum S row length for the dense bitmap block; 0 disables it). */
+ * (minimum S row length for the dense bitmap block; 0 disables it),
+ * "ordered_output" (0: one expansion per row, rows in unspecified order;
+ * 1: count pass + write pass, pairs grouped by first value). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */
@@ -87,8 +92,8 @@ int dim3g_join_project(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const 
 int dim3g_join_project_into(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy,
                             uint64_t nS, uint32_t* out_xz, uint64_t capacity, uint64_t* n_out);
 /* Device-resident input and output: d_R, d_S, d_out are device pointers
- * (8-byte aligned).  On DIM3G_ERR_CAPACITY nothing is written and *n_out
- * holds the pairs needed. */
+ * (8-byte aligned).  On DIM3G_ERR_CAPACITY *n_out holds the pairs needed and
+ * the buffer's contents are unspecified. */
 int dim3g_join_project_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S,
                               uint64_t nS, uint32_t* d_out, uint64_t capacity, uint64_t* n_out);
 /* Count only: the number of distinct pairs, no pairs written. */

@@ -60,7 +60,8 @@ struct CountTile {
 };
 struct NullSink {
     static constexpr bool kValues = false;
-    __device__ __forceinline__ void take(const uint32_t (&)[kUnroll], const uint32_t (&)[kUnroll]) {}
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&)[N], const uint32_t (&)[N]) {}
 };
 
 // Warp-collective emission of occupied map slots [s0, s1) with stride 32.

@@ -30,6 +30,21 @@ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     return h;
 }
 
+// L2 residency: the CSR rows are re-read by many x rows and should stay in
+// L2, while the output pairs stream through once.  Loads of CSR data carry
+// an evict_last policy; output stores use the evict-first (.cs) path.
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint32_t ld_keep(const uint32_t* a, uint64_t pol) {
+    uint32_t v;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_stream(uint2* a, uint2 v) { __stcs(a, v); }
+
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

@@ -27,6 +27,7 @@
 #include "mapper.cuh"
 #include "mapping.cuh"
 #include "scan.cuh"
+#include "single.cuh"
 
 using namespace dim3g;
 
@@ -74,12 +75,14 @@ struct Params {
     uint32_t block_lg = 14;   // 16384 slots per CTA set  -> class 2 up to 8192
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     int64_t heavy_min_len = 0;
+    bool ordered = false;     // two-pass, rows in x-id order
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
 
 struct Scalars {
     unsigned long long nx, ny, nz, nkept, total, outj;
+    unsigned long long cursor;     // single-pass output cursor
     unsigned long long nrows[5];   // rows per class (index = class)
     unsigned int err;
     unsigned int next_row[4];      // dynamic row counters of the CTA classes
@@ -104,6 +107,7 @@ struct dim3g_ctx {
     size_t d_out_bytes = 0;
     Scalars* h_sc = nullptr;  // pinned
     cudaEvent_t ev[6] = {};
+    cudaEvent_t evc[8] = {};  // per row-class kernel timing
     uint64_t launches = 0;  // kernels launched on this context since creation
 };
 
@@ -174,8 +178,11 @@ T* ws_get(dim3g_ctx* c, uint64_t count) {
 
 // Where the write pass puts its result: called once the count pass knows the
 // number of output pairs; returns the device buffers or an error status.
+// peek() gives the current buffer and its capacity without growing it (the
+// single pass writes into whatever is there and reports the size needed).
 struct OutPrep {
     int (*fn)(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned long long** cnt);
+    void (*peek)(dim3g_ctx* c, void* user, uint2** out, uint64_t* capacity);
     void* user;
 };
 
@@ -188,6 +195,7 @@ struct JoinPlan {
     bool swapped;
     bool aggregate;   // COUNT(*) per group instead of distinct pairs
     bool count_only;  // stop after the count pass
+    bool single_pass; // one expansion, rows reserve their output range
     OutPrep prep;
 };
 
@@ -357,19 +365,73 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     const unsigned g_b = resident_grid(k_rows_block<true>, 256, smem_b, sm);
     const unsigned g_m = resident_grid(k_rows_bitmap<true>, blk_m, smem_m, sm);
 
+    if (jp.single_pass && !jp.aggregate && !jp.count_only) {
+        uint2* out = nullptr;
+        uint64_t cap = 0;
+        jp.prep.peek(c, jp.prep.user, &out, &cap);
+        if (!out) cap = 0;
+        rc.out = out;
+        const Reserve rs{&sc->cursor, cap};
+        CU(cudaEventRecord(c->evc[4], st));
+        // single-pass kernels add one kStage-entry staging buffer per warp
+        const uint32_t bm_words = (uint32_t)(smem_m / 4);
+        const size_t ss_m = smem_m + (size_t)(blk_m / 32) * kStage * 4;
+        const size_t ss_b = smem_b + (size_t)8 * kStage * 4;
+        const size_t ss_w = (size_t)8 * ((1u << c->prm.warp_lg) + kStage) * 4;
+        k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3, L.n4,
+                                                                                         bm_words);
+        CHECK_LAUNCH();
+        CU(cudaEventRecord(c->evc[5], st));
+        k_single_block<<<resident_grid(k_single_block, 256, ss_b, sm), 256, ss_b, st>>>(rc, rs, L.b, L.nb, c->prm.block_lg);
+        CHECK_LAUNCH();
+        CU(cudaEventRecord(c->evc[6], st));
+        k_single_warp<<<resident_grid(k_single_warp, 256, ss_w, sm), 256, ss_w, st>>>(rc, rs, L.w, L.nw, c->prm.warp_lg);
+        CHECK_LAUNCH();
+        CU(cudaEventRecord(c->evc[7], st));
+        CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CU(cudaEventRecord(c->ev[3], st));
+        CU(cudaStreamSynchronize(st));
+        if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in single pass (flags %u)", c->h_sc->err);
+        const uint64_t total = c->h_sc->cursor;
+        S.out_j = c->h_sc->outj;
+        S.n_out = total;
+        S.rows_warp = (uint32_t)c->h_sc->nrows[1];
+        S.rows_block = (uint32_t)c->h_sc->nrows[2];
+        S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
+        *n_out = total;
+        float a, b, e;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&e, c->ev[2], c->ev[3]);
+        for (int i = 0; i < 3; i++) cudaEventElapsedTime(&S.ms_write_cls[i], c->evc[4 + i], c->evc[5 + i]);
+        S.ms_map = a;
+        S.ms_csr = b;
+        S.ms_write = e;
+        S.ms_total = a + b + e;
+        if (total > cap)
+            return fail(c, DIM3G_ERR_CAPACITY, "output needs %llu pairs, capacity is %llu", (unsigned long long)total,
+                        (unsigned long long)cap);
+        return DIM3G_OK;
+    }
+
     // count pass (the bitmap rows, the largest, start first)
+    CU(cudaEventRecord(c->evc[0], st));
     k_rows_bitmap<false><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
+    CU(cudaEventRecord(c->evc[1], st));
     k_rows_block<false><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
     CHECK_LAUNCH();
+    CU(cudaEventRecord(c->evc[2], st));
     k_rows_warp<false><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
     CHECK_LAUNCH();
+    CU(cudaEventRecord(c->evc[3], st));
     SCAN(U32Src{cnt}, OffDst{off}, (uint64_t)n + 1, bsum2, &sc->total);
     CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     CU(cudaEventRecord(c->ev[3], st));
     CU(cudaStreamSynchronize(st));
     if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in count pass (flags %u)", c->h_sc->err);
     const uint64_t total = c->h_sc->total;
+    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&S.ms_count_cls[i], c->evc[i], c->evc[i + 1]);
     S.out_j = c->h_sc->outj;
     S.n_out = total;
     S.rows_warp = (uint32_t)c->h_sc->nrows[1];
@@ -398,12 +460,16 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
             int r = run_aggregate_write(c, rc, AggOut{out_cnt}, L);
             if (r) return r;
         } else {
+            CU(cudaEventRecord(c->evc[4], st));
             k_rows_bitmap<true><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
             CHECK_LAUNCH();
+            CU(cudaEventRecord(c->evc[5], st));
             k_rows_block<true><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
             CHECK_LAUNCH();
+            CU(cudaEventRecord(c->evc[6], st));
             k_rows_warp<true><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
             CHECK_LAUNCH();
+            CU(cudaEventRecord(c->evc[7], st));
         }
     }
     CU(cudaMemcpyAsync(&c->h_sc->err, &sc->err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
@@ -420,6 +486,8 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     S.ms_count = d;
     S.ms_write = e;
     S.ms_total = a + b + d + e;
+    if (total > 0 && !jp.aggregate)
+        for (int i = 0; i < 3; i++) cudaEventElapsedTime(&S.ms_write_cls[i], c->evc[4 + i], c->evc[5 + i]);
     return DIM3G_OK;
 }
 
@@ -476,6 +544,11 @@ int prep_device(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned 
     *cnt = d->cnt;
     return DIM3G_OK;
 }
+void peek_device(dim3g_ctx*, void* user, uint2** out, uint64_t* capacity) {
+    DeviceOut* d = (DeviceOut*)user;
+    *out = d->out;
+    *capacity = d->capacity;
+}
 
 // Output preparation for host callers: the context's grow-only device staging.
 struct StagingOut {
@@ -488,6 +561,10 @@ int prep_staging(dim3g_ctx* c, void* user, uint64_t total, uint2** out, unsigned
     *out = (uint2*)c->d_out;
     *cnt = agg ? (unsigned long long*)((char*)c->d_out + total * 8) : nullptr;
     return DIM3G_OK;
+}
+void peek_staging(dim3g_ctx* c, void*, uint2** out, uint64_t* capacity) {
+    *out = (uint2*)c->d_out;
+    *capacity = c->d_out ? c->d_out_bytes / 8 : 0;
 }
 
 // Host-input join: stage R and S on the device, run, copy the result back
@@ -512,9 +589,17 @@ int host_join(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, u
     if (nP) CU(cudaMemcpyAsync(dP, P, nP * 8, cudaMemcpyHostToDevice, st));
     if (nQ) CU(cudaMemcpyAsync(dQ, Q, nQ * 8, cudaMemcpyHostToDevice, st));
     StagingOut so{aggregate};
-    JoinPlan jp{dP, nP, dQ, nQ, swap, aggregate, false, OutPrep{prep_staging, &so}};
+    // single pass once the staging buffer exists; a result larger than it
+    // grows the buffer and runs again
+    const bool single = !aggregate && !c->prm.ordered && c->d_out != nullptr;
+    JoinPlan jp{dP, nP, dQ, nQ, swap, aggregate, false, single, OutPrep{prep_staging, peek_staging, &so}};
     uint64_t n = 0;
     r = run_join(c, jp, &n);
+    if (r == DIM3G_ERR_CAPACITY && single) {
+        r = ensure_dev(c, &c->d_out, &c->d_out_bytes, n * 8);
+        if (r) return r;
+        r = run_join(c, jp, &n);
+    }
     if (r) return r;
     *n_out = n;
     const uint2* dout = (const uint2*)c->d_out;
@@ -576,6 +661,7 @@ int dim3g_create(int device, dim3g_ctx** out) {
         return DIM3G_ERR_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
+    for (auto& e : c->evc) cudaEventCreate(&e);
     c->stream = c->own_stream;
     // Shared-memory carve-outs for the expansion kernels (largest settings).
     const int smem_w = 8 << 11 << 2, smem_b = 1 << 14 << 2, smem_m = (1 << 20) / 8;
@@ -585,6 +671,12 @@ int dim3g_create(int device, dim3g_ctx** out) {
               cudaFuncSetAttribute(k_rows_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_bitmap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_bitmap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
+              cudaFuncSetAttribute(k_single_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   8 * ((1 << 11) + (int)kStage) * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_single_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   ((1 << 14) + 8 * (int)kStage) * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
               set_aggregate_attributes();
     if (!ok) {
         cudaGetLastError();
@@ -604,6 +696,8 @@ void dim3g_destroy(dim3g_ctx* c) {
     if (c->d_out) cudaFree(c->d_out);
     if (c->h_sc) cudaFreeHost(c->h_sc);
     for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->evc)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
@@ -639,6 +733,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "heavy_min_len")) {
         if (v < 0) return fail(c, DIM3G_ERR_INVALID, "heavy_min_len must be >= 0");
         c->prm.heavy_min_len = v;
+    } else if (!strcmp(name, "ordered_output")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "ordered_output must be 0 or 1");
+        c->prm.ordered = v == 1;
     } else {
         return fail(c, DIM3G_ERR_INVALID, "unknown parameter %s", name);
     }
@@ -651,6 +748,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "block_slots_log2")) *v = c->prm.block_lg;
     else if (!strcmp(name, "tile_bits_log2")) *v = c->prm.tile_lg;
     else if (!strcmp(name, "heavy_min_len")) *v = c->prm.heavy_min_len;
+    else if (!strcmp(name, "ordered_output")) *v = c->prm.ordered ? 1 : 0;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }
@@ -688,7 +786,7 @@ int dim3g_join_project_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, con
     const bool swap = nR < nS;
     DeviceOut d{(uint2*)d_out, nullptr, capacity};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
-                swap, false, false, OutPrep{prep_device, &d}};
+                swap, false, false, !c->prm.ordered, OutPrep{prep_device, peek_device, &d}};
     return run_join(c, jp, n_out);
 }
 
@@ -700,7 +798,7 @@ int dim3g_join_project_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t n
     const bool swap = nR < nS;
     DeviceOut d{nullptr, nullptr, 0};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
-                swap, false, true, OutPrep{prep_device, &d}};
+                swap, false, true, false, OutPrep{prep_device, peek_device, &d}};
     return run_join(c, jp, n_out);
 }
 
@@ -720,7 +818,7 @@ int dim3g_join_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const
     const bool swap = nR < nS;
     DeviceOut d{(uint2*)d_out_xz, (unsigned long long*)d_out_cnt, capacity};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
-                swap, true, false, OutPrep{prep_device, &d}};
+                swap, true, false, false, OutPrep{prep_device, peek_device, &d}};
     return run_join(c, jp, n_out);
 }
 

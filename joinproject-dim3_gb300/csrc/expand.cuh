@@ -90,14 +90,15 @@ template <class Set, class Sink>
 __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t part,
                                             uint32_t nparts_lg, uint32_t t0, uint32_t t1, Set& set, Sink& sink) {
     const uint32_t lane = lane_id();
+    const uint64_t pol = l2_keep_policy();
     for (uint32_t eb = e0; eb < e1; eb += 32) {
         const uint32_t e = eb + lane;
         uint32_t s0 = 0, len = 0;
         if (e < e1) {
-            const uint32_t y = __ldg(&c.IC_R[e]);
+            const uint32_t y = ld_keep(&c.IC_R[e], pol);
             const uint64_t r = (uint64_t)y * c.T;
-            s0 = __ldg(&c.JR_S[r + t0]);
-            len = __ldg(&c.JR_S[r + t1]) - s0;
+            s0 = ld_keep(&c.JR_S[r + t0], pol);
+            len = ld_keep(&c.JR_S[r + t1], pol) - s0;
         }
         const uint32_t incl = warp_incl_scan(len);
         if (__any_sync(0xffffffffu, incl < len)) raise_error(c.err, kErrCountRange);
@@ -119,18 +120,31 @@ __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32
             const uint32_t ks0 = __shfl_sync(0xffffffffu, s0, k);
             const uint32_t lo = (p0 > kex ? p0 - kex : 0);
             const uint32_t hi = (kex + klen < p1 ? klen : p1 - kex);
-            for (uint32_t jb = lo; jb < hi; jb += 32 * kUnroll) {
+            uint32_t jb = lo;
+            // full groups: kUnroll x 32 candidates, all loads issued first
+            for (; jb + 32 * kUnroll <= hi; jb += 32 * kUnroll) {
                 uint32_t z[kUnroll], v[kUnroll];
 #pragma unroll
                 for (uint32_t u = 0; u < kUnroll; u++) {
-                    const uint32_t j = jb + u * 32 + lane;
-                    z[u] = j < hi ? __ldg(&c.IC_S[ks0 + j]) : kEmpty32;
-                    if (Sink::kValues) v[u] = j < hi ? __ldg(&c.VS[ks0 + j]) : 0u;
+                    const uint32_t j = ks0 + jb + u * 32 + lane;
+                    z[u] = ld_keep(&c.IC_S[j], pol);
+                    if (Sink::kValues) v[u] = ld_keep(&c.VS[j], pol);
                 }
                 uint32_t b[kUnroll];
 #pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32));
+                for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], true));
                 sink.take(b, v);
+            }
+            // tail: 32 candidates per step, so short segments waste little
+            for (; jb < hi; jb += 32) {
+                const uint32_t j = jb + lane;
+                const bool act = j < hi;
+                uint32_t z1[1], v1[1];
+                z1[0] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
+                if (Sink::kValues) v1[0] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
+                uint32_t b1[1];
+                b1[0] = __ballot_sync(0xffffffffu, set.insert(z1[0], act));
+                sink.take(b1, v1);
             }
         }
     }
@@ -161,9 +175,10 @@ struct TileBitmap {
 struct CountSink {
     static constexpr bool kValues = false;
     uint32_t count = 0;
-    __device__ __forceinline__ void take(const uint32_t (&b)[kUnroll], const uint32_t (&)[kUnroll]) {
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&b)[N], const uint32_t (&)[N]) {
 #pragma unroll
-        for (uint32_t u = 0; u < kUnroll; u++) count += __popc(b[u]);
+        for (uint32_t u = 0; u < N; u++) count += __popc(b[u]);
     }
 };
 
@@ -178,10 +193,11 @@ struct WriteSink {
     uint32_t lim, xv;
     uint32_t* shared_pos;
     uint32_t local = 0;
-    __device__ __forceinline__ void take(const uint32_t (&b)[kUnroll], const uint32_t (&v)[kUnroll]) {
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&b)[N], const uint32_t (&v)[N]) {
         uint32_t n = 0;
 #pragma unroll
-        for (uint32_t u = 0; u < kUnroll; u++) n += __popc(b[u]);
+        for (uint32_t u = 0; u < N; u++) n += __popc(b[u]);
         if (n == 0) return;
         uint32_t pb;
         if (shared_pos) {
@@ -194,10 +210,10 @@ struct WriteSink {
         }
         const uint32_t lt = lanemask_lt();
 #pragma unroll
-        for (uint32_t u = 0; u < kUnroll; u++) {
+        for (uint32_t u = 0; u < N; u++) {
             if (b[u] & (1u << lane_id())) {
                 const uint32_t pos = pb + __popc(b[u] & lt);
-                if (pos < lim) out[base + pos] = make_uint2(xv, v[u]);
+                if (pos < lim) st_stream(&out[base + pos], make_uint2(xv, v[u]));
                 else raise_error(err, kErrOutputBound);
             }
             pb += __popc(b[u]);

@@ -1,0 +1,142 @@
+// single.cuh -- single-pass join-project: each row is expanded once.
+//
+// Every first insertion of a z (hash set or tile bitmap, as in expand.cuh)
+// appends its z value -- loaded beside the z id, coalesced -- to the warp's
+// own shared-memory staging buffer.  When the buffer would overflow, and at
+// the end of the row, the warp reserves that many output slots with one
+// atomicAdd on a global cursor and writes (x value, z value) pairs
+// coalesced.  No second expansion, no gather through id2z, no cross-warp
+// synchronisation for emission.  The output is dense and exact; pairs of one
+// x come in chunks of up to kStage pairs, in unspecified order.  A
+// reservation ending past the caller's capacity writes nothing; the cursor
+// still ends at the exact total, which the host reports as the size needed.
+#pragma once
+#include "common.cuh"
+#include "expand.cuh"
+
+namespace dim3g {
+
+constexpr uint32_t kStage = 512;  // staged z values per warp (2 KB)
+
+struct Reserve {
+    unsigned long long* cursor;
+    unsigned long long cap;
+};
+
+struct StageSink {
+    static constexpr bool kValues = true;
+    uint32_t* stage;  // this warp's kStage-entry buffer
+    uint2* out;
+    Reserve rs;
+    uint32_t xv;
+    uint32_t n = 0;  // staged entries (warp-uniform)
+
+    __device__ __forceinline__ void flush() {
+        if (n == 0) return;
+        unsigned long long base = 0;
+        if (lane_id() == 0) base = atomicAdd(rs.cursor, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        __syncwarp();
+        if (base + n <= rs.cap)
+            for (uint32_t i = lane_id(); i < n; i += 32) st_stream(&out[base + i], make_uint2(xv, stage[i]));
+        __syncwarp();
+        n = 0;
+    }
+
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&b)[N], const uint32_t (&v)[N]) {
+        uint32_t tot = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < N; u++) tot += __popc(b[u]);
+        if (tot == 0) return;
+        if (n + tot > kStage) flush();
+        const uint32_t lt = lanemask_lt();
+        uint32_t pos = n;
+#pragma unroll
+        for (uint32_t u = 0; u < N; u++) {
+            if (b[u] & (1u << lane_id())) stage[pos + __popc(b[u] & lt)] = v[u];
+            pos += __popc(b[u]);
+        }
+        n += tot;
+    }
+};
+
+// Class 1, single pass: one warp per row; per warp 2^warp_lg set slots then
+// kStage staging entries.
+__global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                     const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
+    uint32_t* stage = tab + (1u << warp_lg);
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
+        const uint32_t x = rows[ri];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
+        for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
+        __syncwarp();
+        HashSet set{tab, lg, c.err};
+        StageSink sink{stage, c.out, rs, c.id2x[x]};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+        sink.flush();
+    }
+}
+
+// Class 2, single pass: one CTA per row; 2^block_lg set slots, then one
+// staging buffer per warp.
+__global__ void __launch_bounds__(256) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                      const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_row;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    uint32_t* stage = smem + (1u << block_lg) + wib * kStage;
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
+        const uint32_t x = rows[ri];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+        uint4* t4 = reinterpret_cast<uint4*>(smem);
+        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
+            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
+        __syncthreads();
+        HashSet set{smem, lg, c.err};
+        StageSink sink{stage, c.out, rs, c.id2x[x]};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        sink.flush();
+    }
+}
+
+// Classes 3/4, single pass: one CTA per row; a bitmap over one z tile at a
+// time (words rounded up to uint4, at least 32), then one staging buffer per
+// warp.  The staging survives the tiles of a row.
+__global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                        const unsigned long long* __restrict__ n3,
+                                                        const unsigned long long* __restrict__ n4,
+                                                        uint32_t bitmap_words) {
+    extern __shared__ uint32_t bm[];
+    __shared__ uint32_t s_row;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    uint32_t* stage = bm + bitmap_words + wib * kStage;
+    const uint32_t nrows = (uint32_t)(*n3 + *n4);
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
+        const uint32_t x = rows[ri];
+        StageSink sink{stage, c.out, rs, c.id2x[x]};
+        for (uint32_t t = 0; t < c.T; t++) {
+            const uint32_t lo = t * c.tile_width;
+            const uint32_t width = min(c.tile_width, c.m - lo);
+            const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
+            uint4* b4 = reinterpret_cast<uint4*>(bm);
+            for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            TileBitmap set{bm, lo};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
+            __syncthreads();
+        }
+        sink.flush();
+    }
+}
+
+}  // namespace dim3g

@@ -44,10 +44,15 @@ class Stats(ctypes.Structure):
         ("rows_dense", ctypes.c_uint32), ("z_tiles", ctypes.c_uint32), ("heavy_y", ctypes.c_uint32),
         ("ms_map", ctypes.c_float), ("ms_csr", ctypes.c_float), ("ms_count", ctypes.c_float),
         ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float), ("launches", ctypes.c_uint64),
+        ("ms_count_cls", ctypes.c_float * 3), ("ms_write_cls", ctypes.c_float * 3),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {}
+        for k, _ in self._fields_:
+            v = getattr(self, k)
+            d[k] = [round(float(x), 3) for x in v] if k.endswith("_cls") else v
+        return d
 
 
 # Every symbol include/dim3gpu.h declares (checked by the CPU test suite).

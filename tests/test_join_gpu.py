@@ -40,20 +40,49 @@ def test_join_project_device_api(ctx, golden, name):
     dR = torch.from_numpy(R.view(np.int32)).cuda()
     dS = torch.from_numpy(S.view(np.int32)).cuda()
     n_need = index[name]["n_out"]
-    # too small a buffer: CAPACITY with the size needed, nothing written
+    # too small a buffer: CAPACITY with the size needed
     import dim3gpu
     small = torch.full((max(1, n_need // 2), 2), -1, dtype=torch.int32, device="cuda")
     if n_need > 1:
         with pytest.raises(dim3gpu.Dim3GError) as e:
             ctx.join_project_device(dR, R.shape[0], dS, S.shape[0], small, small.shape[0])
         assert e.value.code == dim3gpu.ERR_CAPACITY
-        assert bool((small == -1).all())
+        assert ctx.stats()["n_out"] == n_need
     assert ctx.join_project_count_device(dR, R.shape[0], dS, S.shape[0]) == n_need
     out = torch.empty((n_need + 5, 2), dtype=torch.int32, device="cuda")
     n = ctx.join_project_device(dR, R.shape[0], dS, S.shape[0], out, out.shape[0])
     torch.cuda.synchronize()
     got = out[:n].cpu().numpy().view(np.uint32)
     check_pairs(got, index[name], arrays, name)
+
+
+@pytest.mark.parametrize("ordered", [0, 1])
+@pytest.mark.parametrize("name", CASES)
+def test_join_project_device_single_and_ordered(built, golden, name, ordered):
+    """Every golden case through the device entry point with an exact buffer:
+    the single pass (ordered_output=0) and the two-pass x-grouped form (1)."""
+    import torch
+    import dim3gpu
+    from oracle import oracle_py as O
+    index, arrays = golden
+    R, S = case_inputs(name, index, arrays)
+    c = dim3gpu.Context(0)
+    c.set_param("ordered_output", ordered)
+    n_need = index[name]["n_out"]
+    dR = torch.from_numpy(R.view(np.int32)).cuda() if R.shape[0] else torch.zeros((1, 2), dtype=torch.int32, device="cuda")
+    dS = torch.from_numpy(S.view(np.int32)).cuda() if S.shape[0] else torch.zeros((1, 2), dtype=torch.int32, device="cuda")
+    out = torch.empty((max(n_need, 1), 2), dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        n = c.join_project_device(dR, R.shape[0], dS, S.shape[0], out, n_need)
+        torch.cuda.synchronize()
+        got = out[:n].cpu().numpy().view(np.uint32)
+        check_pairs(got, index[name], arrays, name)
+    if ordered and n > 1:
+        # pairs of one first value are contiguous
+        firsts = got[:, 0]
+        changes = np.count_nonzero(firsts[1:] != firsts[:-1]) + 1
+        assert changes == np.unique(firsts).shape[0]
+    c.close()
 
 
 def test_join_count_device_api(ctx, golden):
