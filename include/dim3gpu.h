@@ -109,6 +109,28 @@ int dim3g_join_count(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const ui
 int dim3g_join_count_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
                             uint32_t* d_out_xz, uint64_t* d_out_cnt, uint64_t capacity, uint64_t* n_out);
 
+/* ---- allocation-free join-project ------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory where they need the join: code under a custom or
+ * fixed-budget allocator, hosts that preallocate everything at start-up,
+ * and pipelines that cannot afford the synchronisation an allocation may
+ * bring.  Device inputs, the caller's output buffer, and all scratch in one
+ * fixed array inside the library (about 19 MB, held on every GPU that loads
+ * the library until the process exits); it calls no allocating routine.
+ * Limits: the larger relation holds at most DIM3G_NOALLOC_MAX_TUPLES tuples
+ * and the result at most DIM3G_NOALLOC_MAX_PAIRS distinct pairs; beyond
+ * either it returns DIM3G_ERR_UNSUPPORTED.  The first call on a device looks
+ * up the array's device address (once per device, with that device
+ * current); make that first call before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race, so serialise them.  The
+ * result set, *n_out and DIM3G_ERR_CAPACITY are as for
+ * dim3g_join_project_device.  cuda_stream is a cudaStream_t (NULL: the
+ * default stream), synchronised before the call returns. */
+#define DIM3G_NOALLOC_MAX_TUPLES (1u << 18)
+#define DIM3G_NOALLOC_MAX_PAIRS (1u << 20)
+int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
+                               uint32_t* d_out, uint64_t capacity, uint64_t* n_out, void* cuda_stream);
+
 /* ---- L+S mapper -----------------------------------------------------
  * Replaces LS_mapper<T,H,Tcounter> (Include/L+S_mapper.hpp:11-160): a GPU
  * value -> dense id map.  insert() gives every key its existing id or the

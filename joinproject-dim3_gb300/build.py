@@ -41,7 +41,8 @@ def commands(force=False):
     cmds = []
     gpu_deps = _sources(".cu") + _sources(".cuh") + [os.path.join(REPO, "include", "dim3gpu.h")]
     if force or _stale(GPU_SO, gpu_deps):
-        cmds.append([_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "dim3gpu.cu"), "-o", GPU_SO])
+        cmds.append([_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "dim3gpu.cu"), os.path.join(CSRC, "noalloc.cu"),
+                                              "-o", GPU_SO])
     gen_deps = [os.path.join(CSRC, "dim3gen.c"), os.path.join(CSRC, "dim3gen.h")]
     if force or _stale(GEN_SO, gen_deps):
         cmds.append(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",

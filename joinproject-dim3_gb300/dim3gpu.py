@@ -63,6 +63,7 @@ EXPORTS = [
     "dim3g_join_project_count_device", "dim3g_join_count", "dim3g_join_count_device",
     "dim3g_mapper_create", "dim3g_mapper_destroy", "dim3g_mapper_insert", "dim3g_mapper_find",
     "dim3g_mapper_size", "dim3g_mapper_clear", "dim3g_mapper_set_cnt",
+    "dim3g_join_project_noalloc",
 ]
 
 _lib = None
