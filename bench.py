@@ -230,9 +230,10 @@ def run_gpu(args, rank, world, local_rank):
                "ms_per_step": round(e2e_s * 1e3, 3)}
     st = ctx.stats()
     peak, peak_kind = load_peaks()
-    # Dominant kernel: the write pass of the expansion (one launch per row
-    # class).  Algorithmic bytes per launch: 4 B per candidate read + 8 B per
-    # distinct pair written.
+    # Dominant kernel: the single-pass expansion (one launch per row class:
+    # k_single_bitmap / k_single_block / k_single_warp), timed by the
+    # library's CUDA events on its stream.  Algorithmic bytes per launch:
+    # 4 B per candidate z id read + 8 B per distinct pair written.
     ms_w = sum(ms_write) / len(ms_write)
     alg_bytes = 4 * st["out_j"] + 8 * n_out
     achieved = alg_bytes / (ms_w / 1e3) / 1e9
@@ -245,7 +246,7 @@ def run_gpu(args, rank, world, local_rank):
                    "parallelism": "replicas" if world > 1 else "single"},
         "phases_ms": {k: round(v / args.steps, 3) for k, v in ms_phase.items()},
         "e2e": e2e,
-        "roofline": {"bound": "hbm", "kernel": "expand write pass (k_rows_warp/block/bitmap<true>)",
+        "roofline": {"bound": "hbm", "kernel": "single-pass expansion (k_single_bitmap, k_single_block, k_single_warp)",
                      "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": args.traffic,
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(ms_w, 3)},

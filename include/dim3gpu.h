@@ -67,7 +67,7 @@ void dim3g_destroy(dim3g_ctx* ctx);
 int dim3g_set_stream(dim3g_ctx* ctx, void* cuda_stream);
 const char* dim3g_last_error(const dim3g_ctx* ctx);
 int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
-/* Tuning knobs, validated on set: "warp_slots_log2" (5..11, warp-class hash
+/* Tuning knobs, validated on set: "warp_slots_log2" (5..14, warp-class hash
  * set size), "block_slots_log2" (8..14, block-class hash set size),
  * "tile_bits_log2" (10..20, bitmap-class z tile width), "heavy_min_len"
  * (minimum S row length for the dense bitmap block; 0 disables it),

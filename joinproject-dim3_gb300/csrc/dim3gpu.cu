@@ -73,6 +73,7 @@ struct Arena {
 struct Params {
     uint32_t warp_lg = 11;    // 2048 slots per warp set  -> class 1 up to 1024
     uint32_t block_lg = 14;   // 16384 slots per CTA set  -> class 2 up to 8192
+    uint32_t block_threads = 512;  // CTA width of the class-2 kernels
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     int64_t heavy_min_len = 0;
     bool ordered = false;     // two-pass, rows in x-id order
@@ -205,6 +206,15 @@ struct RowLists {
     const unsigned long long *nw, *nb, *n3, *n4;        // their sizes (device)
 };
 int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const RowLists& L);
+
+// Warps per CTA of a warp-per-row kernel whose warps each own per_warp
+// bytes of shared memory: up to 8, within about half an SM's shared memory
+// so two CTAs fit per SM.
+constexpr size_t kWarpCtaSmem = 112 * 1024;
+inline uint32_t warps_per_cta(size_t per_warp) {
+    size_t w = kWarpCtaSmem / per_warp;
+    return (uint32_t)(w < 1 ? 1 : (w > 8 ? 8 : w));
+}
 
 // Grid of a persistent / grid-stride kernel: resident CTAs per SM x SMs.
 template <class K>
@@ -356,13 +366,15 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     // Row counts are read on the device; grids are resident CTAs x SMs.
     const RowLists L{list_w, list_b, list_m, &sc->nrows[1], &sc->nrows[2], &sc->nrows[3], &sc->nrows[4]};
     rc.next_row = sc->next_row;
-    const size_t smem_w = (size_t)8 << c->prm.warp_lg << 2;
+    const uint32_t wpc = warps_per_cta((size_t)4 << c->prm.warp_lg);  // warp-class CTA width
+    const size_t smem_w = (size_t)wpc << c->prm.warp_lg << 2;
     const size_t smem_b = (size_t)1 << c->prm.block_lg << 2;
     size_t smem_m = (size_t)((((tile_width + 31) / 32) + 3) / 4) * 16;  // whole uint4 words (cleared as uint4)
     if (smem_m < 128) smem_m = 128;  // idle lanes touch words 0..31
     const int blk_m = tile_width > (1u << 19) ? 1024 : 512;
-    const unsigned g_w = resident_grid(k_rows_warp<true>, 256, smem_w, sm);
-    const unsigned g_b = resident_grid(k_rows_block<true>, 256, smem_b, sm);
+    const unsigned g_w = resident_grid(k_rows_warp<true>, 32 * wpc, smem_w, sm);
+    const int blk_b = (int)c->prm.block_threads;
+    const unsigned g_b = resident_grid(k_rows_block<true>, blk_b, smem_b, sm);
     const unsigned g_m = resident_grid(k_rows_bitmap<true>, blk_m, smem_m, sm);
 
     if (jp.single_pass && !jp.aggregate && !jp.count_only) {
@@ -376,16 +388,19 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         // single-pass kernels add one kStage-entry staging buffer per warp
         const uint32_t bm_words = (uint32_t)(smem_m / 4);
         const size_t ss_m = smem_m + (size_t)(blk_m / 32) * kStage * 4;
-        const size_t ss_b = smem_b + (size_t)8 * kStage * 4;
-        const size_t ss_w = (size_t)8 * ((1u << c->prm.warp_lg) + kStage) * 4;
+        const size_t ss_b = smem_b + (size_t)(blk_b / 32) * kStage * 4;
+        const uint32_t wps = warps_per_cta(((size_t)(1u << c->prm.warp_lg) + kStage) * 4);
+        const size_t ss_w = (size_t)wps * ((1u << c->prm.warp_lg) + kStage) * 4;
         k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3, L.n4,
                                                                                          bm_words);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[5], st));
-        k_single_block<<<resident_grid(k_single_block, 256, ss_b, sm), 256, ss_b, st>>>(rc, rs, L.b, L.nb, c->prm.block_lg);
+        k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(rc, rs, L.b, L.nb,
+                                                                                          c->prm.block_lg);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[6], st));
-        k_single_warp<<<resident_grid(k_single_warp, 256, ss_w, sm), 256, ss_w, st>>>(rc, rs, L.w, L.nw, c->prm.warp_lg);
+        k_single_warp<<<resident_grid(k_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(rc, rs, L.w, L.nw,
+                                                                                           c->prm.warp_lg);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[7], st));
         CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
@@ -419,10 +434,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     k_rows_bitmap<false><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
     CU(cudaEventRecord(c->evc[1], st));
-    k_rows_block<false><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
+    k_rows_block<false><<<g_b, blk_b, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
     CHECK_LAUNCH();
     CU(cudaEventRecord(c->evc[2], st));
-    k_rows_warp<false><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
+    k_rows_warp<false><<<g_w, 32 * wpc, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
     CHECK_LAUNCH();
     CU(cudaEventRecord(c->evc[3], st));
     SCAN(U32Src{cnt}, OffDst{off}, (uint64_t)n + 1, bsum2, &sc->total);
@@ -464,10 +479,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
             k_rows_bitmap<true><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
             CHECK_LAUNCH();
             CU(cudaEventRecord(c->evc[5], st));
-            k_rows_block<true><<<g_b, 256, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
+            k_rows_block<true><<<g_b, blk_b, smem_b, st>>>(rc, L.b, L.nb, c->prm.block_lg);
             CHECK_LAUNCH();
             CU(cudaEventRecord(c->evc[6], st));
-            k_rows_warp<true><<<g_w, 256, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
+            k_rows_warp<true><<<g_w, 32 * wpc, smem_w, st>>>(rc, L.w, L.nw, c->prm.warp_lg);
             CHECK_LAUNCH();
             CU(cudaEventRecord(c->evc[7], st));
         }
@@ -494,20 +509,22 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
 int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const RowLists& L) {
     cudaStream_t st = c->stream;
     const int sm = c->sm_count;
-    const size_t smem_w = (size_t)8 << (c->prm.warp_lg + 1) << 2;
+    const uint32_t wpa = warps_per_cta((size_t)8 << c->prm.warp_lg);
+    const size_t smem_w = (size_t)wpa << (c->prm.warp_lg + 1) << 2;
     const size_t smem_b = (size_t)2 << c->prm.block_lg << 2;
     const size_t smem_m = (size_t)rc.tile_width * 4;
     k_agg_tile<<<resident_grid(k_agg_tile, 1024, smem_m, sm), 1024, smem_m, st>>>(rc, ao, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
     k_agg_block<<<resident_grid(k_agg_block, 256, smem_b, sm), 256, smem_b, st>>>(rc, ao, L.b, L.nb, c->prm.block_lg);
     CHECK_LAUNCH();
-    k_agg_warp<<<resident_grid(k_agg_warp, 256, smem_w, sm), 256, smem_w, st>>>(rc, ao, L.w, L.nw, c->prm.warp_lg);
+    k_agg_warp<<<resident_grid(k_agg_warp, 32 * wpa, smem_w, sm), 32 * wpa, smem_w, st>>>(rc, ao, L.w, L.nw,
+                                                                                         c->prm.warp_lg);
     CHECK_LAUNCH();
     return DIM3G_OK;
 }
 
 bool set_aggregate_attributes() {
-    return cudaFuncSetAttribute(k_agg_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 12 << 2) == cudaSuccess &&
+    return cudaFuncSetAttribute(k_agg_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess &&
            cudaFuncSetAttribute(k_agg_block, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 << 14 << 2) == cudaSuccess &&
            cudaFuncSetAttribute(k_agg_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (1 << kAggTileLg) * 4) == cudaSuccess;
 }
@@ -665,16 +682,16 @@ int dim3g_create(int device, dim3g_ctx** out) {
     c->stream = c->own_stream;
     // Shared-memory carve-outs for the expansion kernels (largest settings).
     const int smem_w = 8 << 11 << 2, smem_b = 1 << 14 << 2, smem_m = (1 << 20) / 8;
-    bool ok = cudaFuncSetAttribute(k_rows_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_w) == cudaSuccess &&
-              cudaFuncSetAttribute(k_rows_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_w) == cudaSuccess &&
+    const int smem_wmax = 200 * 1024;
+    bool ok = cudaFuncSetAttribute(k_rows_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_wmax) == cudaSuccess &&
+              cudaFuncSetAttribute(k_rows_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_wmax) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_bitmap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_bitmap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_m) == cudaSuccess &&
-              cudaFuncSetAttribute(k_single_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   8 * ((1 << 11) + (int)kStage) * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_single_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_wmax) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   ((1 << 14) + 8 * (int)kStage) * 4) == cudaSuccess &&
+                                   ((1 << 14) + 32 * (int)kStage) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
               set_aggregate_attributes();
@@ -721,7 +738,8 @@ int dim3g_get_stats(const dim3g_ctx* c, dim3g_stats* out) {
 int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     if (!c || !name) return DIM3G_ERR_INVALID;
     if (!strcmp(name, "warp_slots_log2")) {
-        if (v < 5 || v > 11) return fail(c, DIM3G_ERR_INVALID, "warp_slots_log2 must be in 5..11");
+        if (v < 5 || v > 14) return fail(c, DIM3G_ERR_INVALID, "warp_slots_log2 must be in 5..14");
+        if ((uint32_t)v > c->prm.block_lg) c->prm.block_lg = (uint32_t)v;
         c->prm.warp_lg = (uint32_t)v;
     } else if (!strcmp(name, "block_slots_log2")) {
         if (v < 8 || v > 14) return fail(c, DIM3G_ERR_INVALID, "block_slots_log2 must be in 8..14");
@@ -733,6 +751,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "heavy_min_len")) {
         if (v < 0) return fail(c, DIM3G_ERR_INVALID, "heavy_min_len must be >= 0");
         c->prm.heavy_min_len = v;
+    } else if (!strcmp(name, "block_threads")) {
+        if (v != 256 && v != 512 && v != 1024) return fail(c, DIM3G_ERR_INVALID, "block_threads must be 256, 512 or 1024");
+        c->prm.block_threads = (uint32_t)v;
     } else if (!strcmp(name, "ordered_output")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "ordered_output must be 0 or 1");
         c->prm.ordered = v == 1;
@@ -749,6 +770,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "tile_bits_log2")) *v = c->prm.tile_lg;
     else if (!strcmp(name, "heavy_min_len")) *v = c->prm.heavy_min_len;
     else if (!strcmp(name, "ordered_output")) *v = c->prm.ordered ? 1 : 0;
+    else if (!strcmp(name, "block_threads")) *v = c->prm.block_threads;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

@@ -135,16 +135,23 @@ __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32
                 for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], true));
                 sink.take(b, v);
             }
-            // tail: 32 candidates per step, so short segments waste little
-            for (; jb < hi; jb += 32) {
-                const uint32_t j = jb + lane;
-                const bool act = j < hi;
-                uint32_t z1[1], v1[1];
-                z1[0] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
-                if (Sink::kValues) v1[0] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
-                uint32_t b1[1];
-                b1[0] = __ballot_sync(0xffffffffu, set.insert(z1[0], act));
-                sink.take(b1, v1);
+            // tail (< kUnroll x 32 left): all its loads issued together, so
+            // one load latency per segment tail; steps past the end are
+            // skipped warp-uniformly
+            if (jb < hi) {
+                uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+                for (uint32_t u = 0; u < kUnroll; u++) {
+                    const uint32_t j = jb + u * 32 + lane;
+                    const bool act = j < hi;
+                    z[u] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
+                    if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
+                }
+                uint32_t b[kUnroll];
+#pragma unroll
+                for (uint32_t u = 0; u < kUnroll; u++)
+                    b[u] = (jb + u * 32 < hi) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
+                sink.take(b, v);
             }
         }
     }
@@ -258,7 +265,7 @@ __global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __r
 
 // Class 2: one CTA per row, 2^block_lg slots.
 template <bool WRITE>
-__global__ void __launch_bounds__(256) k_rows_block(RowCtx c, const uint32_t* __restrict__ rows,
+__global__ void __launch_bounds__(1024) k_rows_block(RowCtx c, const uint32_t* __restrict__ rows,
                                                     const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_count, s_row;

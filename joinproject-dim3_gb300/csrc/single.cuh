@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs, const
 
 // Class 2, single pass: one CTA per row; 2^block_lg set slots, then one
 // staging buffer per warp.
-__global__ void __launch_bounds__(256) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+__global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
                                                       const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row;
