@@ -57,6 +57,8 @@ typedef struct {
     uint64_t launches;         /* kernels launched on this context since creation */
     float ms_count_cls[3];     /* count pass device ms per row kernel: bitmap, block, warp */
     float ms_write_cls[3];     /* write pass device ms per row kernel: bitmap, block, warp */
+    uint64_t out_j_cls[3];     /* candidates (join tuples) per row kernel: bitmap, block, warp */
+    uint64_t n_out_cls[3];     /* distinct pairs per row kernel (single pass): bitmap, block, warp */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */

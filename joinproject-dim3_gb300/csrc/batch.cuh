@@ -1,0 +1,655 @@
+// batch.cuh -- many joins per launch.
+//
+// Relation set: for every relation r of a set (tuples (f, y), f the first
+// column) one segmented pass builds, for all relations at once,
+//   TF, TY      value -> id tables (f and y), ids dense per relation
+//   CSR by f    JRf over the global f-id space, ICf = global y ids
+//               (the relation in the role of R)
+//   CSR by (y, f tile)  JRy over a per-relation key space y*T + tile (plus
+//               T empty sentinel keys), ICy = local f ids, VSy = f values
+//               beside them (the relation in the role of S)
+// Every relation's ids and keys are local; the set lays them out
+// relation-major, so one prefix sum over a whole pool gives every
+// relation's CSR at once (a relation's first global position is the tuple
+// count of the relations before it).
+//
+// Query set: joins (P, Q) of relations of a set.  Per query a y map (P's y
+// ids -> Q's y ids, or Q's empty sentinel row), P's CSR re-expressed in Q's
+// y ids, per-row work and classes; then the row kernels of the single
+// relation path run over the rows of all queries, each row fetching its
+// query's context.  Kernels take their segment offsets from device memory,
+// so a fixed launch sequence (capturable in a CUDA graph) serves any batch
+// of a given shape.
+#pragma once
+#include "aggregate.cuh"
+#include "common.cuh"
+#include "expand.cuh"
+#include "mapping.cuh"
+#include "single.cuh"
+
+namespace dim3g {
+
+// Largest s in [0, n) with off[s] <= i (off[0..n] nondecreasing, off[0] = 0,
+// i < off[n]): the segment holding element i, skipping empty segments.
+__device__ __forceinline__ uint32_t seg_find(const uint64_t* __restrict__ off, uint32_t n, uint64_t i) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&off[mid]) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Per-thread cached segment lookup for loops over contiguous elements.
+struct SegCursor {
+    const uint64_t* off;
+    uint32_t n;
+    uint32_t s = 0;
+    uint64_t lo = 1, hi = 0;
+    __device__ __forceinline__ uint32_t at(uint64_t i) {
+        if (i < lo || i >= hi) {
+            s = seg_find(off, n, i);
+            lo = __ldg(&off[s]);
+            hi = __ldg(&off[s + 1]);
+        }
+        return s;
+    }
+};
+
+// CTA-contiguous element ranges: CTA b covers [b*per, (b+1)*per) in rounds
+// of blockDim, so a thread's segment changes rarely.
+#define DIM3G_FOR_CHUNK(i, n)                                                           \
+    const uint64_t per_ = ((n) + gridDim.x - 1) / gridDim.x;                            \
+    const uint64_t c0_ = (uint64_t)blockIdx.x * per_;                                   \
+    const uint64_t c1_ = c0_ + per_ < (n) ? c0_ + per_ : (n);                           \
+    for (uint64_t i = c0_ + threadIdx.x; i < c1_; i += blockDim.x)
+
+// Adds pred over the calling lanes to ctr[s], one atomic per group of lanes
+// sharing s.
+__device__ __forceinline__ void warp_count_by_seg(unsigned long long* ctr, uint32_t s, bool pred) {
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, s);
+    const unsigned b = __ballot_sync(act, pred) & grp;
+    if (b && (int)lane_id() == __ffs(grp) - 1) atomicAdd(&ctr[s], (unsigned long long)__popc(b));
+}
+
+// ------------------------------------------------------------ relation set
+struct RelIn {
+    const uint2* pairs;  // (f, y) tuples, device
+    uint64_t n;
+};
+
+// Per-relation layout, computed on the device once the id counts are known.
+struct RelDev {
+    uint64_t nt;        // tuples
+    uint64_t tup_off;   // first position in the tuple-indexed pools
+    uint64_t tab_off;   // first slot in TF / TY
+    uint64_t tab_cap;   // slots per table (power of two)
+    uint64_t nf, ny;    // distinct f, distinct y
+    uint64_t fbase, ybase;  // first global f id / y id
+    uint64_t yt_base;   // first key of the (y, f tile) key space
+    uint32_t T, tile_shift, tile_width, pad;
+};
+
+// Pools of one relation set (device pointers).
+struct RelPools {
+    const RelIn* in;
+    RelDev* rel;
+    const uint64_t* tup_off;  // nrel + 1
+    const uint64_t* tab_off;  // nrel + 1
+    uint32_t nrel;
+    uint64_t ntot;            // sum of tuples
+    unsigned long long* TF;
+    unsigned long long* TY;
+    unsigned long long* nf_cnt;  // nrel
+    unsigned long long* ny_cnt;  // nrel
+    uint32_t* id2f;           // by global f id
+    uint32_t* id2y;           // by global y id
+    uint2* Pm;                // (global f id, global y id) per tuple
+    uint32_t* degF;           // ntot + 1
+    uint32_t* JRf;            // ntot + 1, global positions
+    uint32_t* curF;
+    uint32_t* ICf;            // global y ids
+    uint32_t* cnt_yt;         // yt_cap
+    uint32_t* JRy;            // yt_cap, global positions
+    uint32_t* curY;
+    uint64_t yt_cap;
+    uint32_t* ICy;            // local f ids
+    uint32_t* VSy;            // f values
+    uint32_t* err;            // device error flags of the set
+    unsigned long long* yt_need;  // keys the layout needs (+1)
+};
+
+__device__ __forceinline__ DevTable rel_table(unsigned long long* pool, const RelDev& r) {
+    return DevTable{pool + r.tab_off, r.tab_cap - 1};
+}
+
+__global__ void k_ix_insert(RelPools P) {
+    SegCursor sc{P.tup_off, P.nrel};
+    DIM3G_FOR_CHUNK(i, P.ntot) {
+        const uint32_t r = sc.at(i);
+        const uint2 t = P.in[r].pairs[i - sc.lo];
+        const uint64_t to = __ldg(&P.tab_off[r]), cap = __ldg(&P.tab_off[r + 1]) - to;
+        const bool nf = table_insert(DevTable{P.TF + to, cap - 1}, t.x, P.err);
+        const bool ny = table_insert(DevTable{P.TY + to, cap - 1}, t.y, P.err);
+        warp_count_by_seg(P.nf_cnt, r, nf);
+        warp_count_by_seg(P.ny_cnt, r, ny);
+    }
+}
+
+// One CTA: per-relation id bases, z tiling and (y, tile) key ranges.
+__global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t tile_lg) {
+    __shared__ uint64_t sm[1024 / 32 + 1];
+    uint64_t cf = 0, cy = 0, ck = 0;
+    for (uint32_t b = 0; b < P.nrel; b += 1024) {
+        const uint32_t r = b + threadIdx.x;
+        uint64_t nf = 0, ny = 0, T = 1, keys = 0;
+        if (r < P.nrel) {
+            nf = P.nf_cnt[r];
+            ny = P.ny_cnt[r];
+            T = nf > (1ull << tile_lg) ? (nf + (1ull << tile_lg) - 1) >> tile_lg : 1;
+            keys = ny * T + T;  // T sentinel keys: y id ny has no tuples
+        }
+        uint64_t tf, ty, tk;
+        const uint64_t ef = block_excl_scan<1024>(nf, sm, &tf);
+        const uint64_t ey = block_excl_scan<1024>(ny, sm, &ty);
+        const uint64_t ek = block_excl_scan<1024>(keys, sm, &tk);
+        if (r < P.nrel) {
+            RelDev d;
+            d.nt = P.in[r].n;
+            d.tup_off = P.tup_off[r];
+            d.tab_off = P.tab_off[r];
+            d.tab_cap = P.tab_off[r + 1] - P.tab_off[r];
+            d.nf = nf;
+            d.ny = ny;
+            d.fbase = cf + ef;
+            d.ybase = cy + ey;
+            d.yt_base = ck + ek;
+            d.T = (uint32_t)T;
+            d.tile_shift = T > 1 ? tile_lg : 31;
+            d.tile_width = T > 1 ? (1u << tile_lg) : (uint32_t)(nf > 0 ? nf : 1);
+            d.pad = 0;
+            P.rel[r] = d;
+        }
+        cf += tf;
+        cy += ty;
+        ck += tk;
+    }
+    if (threadIdx.x == 0) {
+        *P.yt_need = ck + 1;
+        if (ck + 1 > P.yt_cap) raise_error(P.err, kErrTableFull);
+    }
+}
+
+// Tuples -> (global f id, global y id); degree of f; count of (y, f tile).
+__global__ void k_ix_map(RelPools P) {
+    if (*P.yt_need > P.yt_cap) return;  // layout overflow: the host regrows
+    SegCursor sc{P.tup_off, P.nrel};
+    DIM3G_FOR_CHUNK(i, P.ntot) {
+        const uint32_t r = sc.at(i);
+        const RelDev& d = P.rel[r];
+        const uint2 t = P.in[r].pairs[i - sc.lo];
+        const uint32_t fid = table_find(rel_table(P.TF, d), t.x);
+        const uint32_t yid = table_find(rel_table(P.TY, d), t.y);
+        P.Pm[i] = make_uint2(fid, yid);
+        atomicAdd(&P.degF[fid], 1u);
+        const uint64_t key = d.yt_base + (uint64_t)(yid - d.ybase) * d.T + ((fid - d.fbase) >> d.tile_shift);
+        atomicAdd(&P.cnt_yt[key], 1u);
+    }
+}
+
+__global__ void k_ix_scatter(RelPools P) {
+    if (*P.yt_need > P.yt_cap) return;
+    SegCursor sc{P.tup_off, P.nrel};
+    DIM3G_FOR_CHUNK(i, P.ntot) {
+        const uint32_t r = sc.at(i);
+        const RelDev& d = P.rel[r];
+        const uint2 pm = P.Pm[i];
+        const uint32_t pos = atomicAdd(&P.curF[pm.x], 1u);
+        P.ICf[pos] = pm.y;
+        const uint32_t fl = pm.x - (uint32_t)d.fbase;
+        const uint64_t key = d.yt_base + (uint64_t)(pm.y - d.ybase) * d.T + (fl >> d.tile_shift);
+        const uint32_t p2 = atomicAdd(&P.curY[key], 1u);
+        P.ICy[p2] = fl;
+        P.VSy[p2] = P.in[r].pairs[i - sc.lo].x;
+    }
+}
+
+// --------------------------------------------------------------- query set
+enum QueryOp : uint32_t { kOpProject = 0, kOpCount = 1 };
+
+struct QueryIn {
+    uint32_t p, q;        // relation ids: P drives the rows, Q is probed
+    uint32_t op;          // QueryOp
+    uint32_t pad;
+    uint2* out;           // (P.f, Q.f) pairs
+    unsigned long long* out_cnt;  // counts (kOpCount)
+    uint64_t cap;         // pairs the output holds
+};
+
+// Per-query results, copied back after the batch.
+struct QueryRes {
+    unsigned long long n_out;   // pairs written (or needed when > cap)
+    unsigned long long out_j;   // candidates
+    unsigned long long rows[3]; // rows per kernel class: bitmap, block, warp
+    uint32_t err, nx, ny, nz;
+};
+
+struct QueryPools {
+    const RelDev* rel;
+    const QueryIn* qin;
+    uint32_t nq;
+    const uint64_t* qt_off;    // nq + 1: prefix of P tuple counts (y map, P entries)
+    const uint64_t* qrow_off;  // nq + 1: prefix of P tuple counts + 1 (rows)
+    uint64_t ntot, nrows;
+    const unsigned long long* TY;
+    const uint32_t* id2f;
+    const uint32_t* id2y;
+    const uint32_t* JRf;
+    const uint32_t* ICf;
+    const uint32_t* JRy;
+    const uint32_t* ICy;
+    const uint32_t* VSy;
+    uint32_t* ymap;   // ntot
+    uint32_t* ICq;    // ntot: P entries as Q y ids
+    uint32_t* JRq;    // nrows: P row pointers, relative
+    uint32_t* ucap;   // nrows
+    uint8_t* cls;     // nrows
+    RowCtx* rc;       // nq
+    Reserve* rs;      // nq
+    QueryRes* res;    // nq
+};
+
+// y map: y id of P -> y id of Q, or Q's sentinel y id (no tuples).
+__global__ void k_q_ymap(QueryPools Q) {
+    SegCursor sc{Q.qt_off, Q.nq};
+    DIM3G_FOR_CHUNK(i, Q.ntot) {
+        const uint32_t qi = sc.at(i);
+        const QueryIn qn = Q.qin[qi];
+        const RelDev& p = Q.rel[qn.p];
+        const RelDev& q = Q.rel[qn.q];
+        const uint64_t y = i - sc.lo;
+        if (y >= p.ny) continue;
+        const uint32_t g = table_find(DevTable{(unsigned long long*)Q.TY + q.tab_off, q.tab_cap - 1},
+                                      Q.id2y[p.ybase + y]);
+        Q.ymap[i] = g == kNotFound ? (uint32_t)q.ny : g - (uint32_t)q.ybase;
+    }
+}
+
+// P's CSR entries as Q y ids.
+__global__ void k_q_entries(QueryPools Q) {
+    SegCursor sc{Q.qt_off, Q.nq};
+    DIM3G_FOR_CHUNK(i, Q.ntot) {
+        const uint32_t qi = sc.at(i);
+        const RelDev& p = Q.rel[Q.qin[qi].p];
+        const uint32_t yg = Q.ICf[p.tup_off + (i - sc.lo)];
+        Q.ICq[i] = Q.ymap[sc.lo + (yg - p.ybase)];
+    }
+}
+
+// P's row pointers relative to P's first entry.
+__global__ void k_q_rows(QueryPools Q) {
+    SegCursor sc{Q.qrow_off, Q.nq};
+    DIM3G_FOR_CHUNK(i, Q.nrows) {
+        const uint32_t qi = sc.at(i);
+        const RelDev& p = Q.rel[Q.qin[qi].p];
+        const uint64_t x = i - sc.lo;
+        if (x <= p.nf) Q.JRq[i] = Q.JRf[p.fbase + x] - (uint32_t)p.tup_off;
+    }
+}
+
+// One thread per query: its row context and output reservation.
+__global__ void k_q_setup(QueryPools Q) {
+    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= Q.nq) return;
+    const QueryIn qn = Q.qin[qi];
+    const RelDev& p = Q.rel[qn.p];
+    const RelDev& q = Q.rel[qn.q];
+    RowCtx c{};
+    c.JR_R = Q.JRq + Q.qrow_off[qi];
+    c.IC_R = Q.ICq + Q.qt_off[qi];
+    c.JR_S = Q.JRy + q.yt_base;
+    c.IC_S = Q.ICy;
+    c.VS = Q.VSy;
+    c.T = q.T;
+    c.tile_width = q.tile_width;
+    c.m = (uint32_t)q.nf;
+    c.ucap = Q.ucap + Q.qrow_off[qi];
+    c.cnt = nullptr;
+    c.off = nullptr;
+    c.id2x = Q.id2f + p.fbase;
+    c.id2z = Q.id2f + q.fbase;
+    c.out = qn.out;
+    c.err = &Q.res[qi].err;
+    c.next_row = nullptr;
+    Q.rc[qi] = c;
+    Q.rs[qi] = Reserve{&Q.res[qi].n_out, qn.cap};
+    QueryRes r{};
+    r.nx = (uint32_t)p.nf;
+    r.ny = (uint32_t)p.ny;
+    r.nz = (uint32_t)q.nf;
+    Q.res[qi] = r;
+}
+
+// Per-row work and class (1..4 project, 5..8 COUNT, 0 empty); one warp per
+// row of the row space.
+__global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b) {
+    const uint32_t lane = lane_id();
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t per = (Q.nrows + nwarps - 1) / nwarps;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t g0 = gw * per, g1 = g0 + per < Q.nrows ? g0 + per : Q.nrows;
+    SegCursor sc{Q.qrow_off, Q.nq};
+    unsigned long long acc = 0;
+    uint32_t acc_q = 0xFFFFFFFFu;
+    for (uint64_t g = g0; g < g1; g++) {
+        const uint32_t qi = sc.at(g);
+        if (qi != acc_q) {
+            if (lane == 0 && acc) atomicAdd(&Q.res[acc_q].out_j, acc);
+            acc = 0;
+            acc_q = qi;
+        }
+        const RowCtx& c = Q.rc[qi];
+        const uint64_t x = g - sc.lo;
+        const uint32_t nf = Q.res[qi].nx;
+        if (x >= nf) {
+            if (lane == 0) Q.cls[g] = 0;
+            continue;
+        }
+        const uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
+        unsigned long long w = 0;
+        for (uint32_t e = e0 + lane; e < e1; e += 32) {
+            const uint64_t r = (uint64_t)c.IC_R[e] * c.T;
+            w += c.JR_S[r + c.T] - c.JR_S[r];
+        }
+        w = warp_sum(w);
+        if (lane == 0) {
+            const uint32_t u = (uint32_t)(w < c.m ? w : c.m);
+            Q.ucap[g] = u;
+            uint32_t k = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
+            if (k && Q.qin[qi].op == kOpCount) {
+                k += 4;
+                if (w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
+            }
+            Q.cls[g] = (uint8_t)k;
+            acc += w;
+        }
+    }
+    if (lane == 0 && acc) atomicAdd(&Q.res[acc_q].out_j, acc);
+}
+
+// Row g of the row space -> (query, local row).
+__device__ __forceinline__ uint32_t query_of_row(const QueryPools& Q, uint32_t g, uint32_t* x) {
+    const uint32_t qi = seg_find(Q.qrow_off, Q.nq, g);
+    *x = g - (uint32_t)Q.qrow_off[qi];
+    return qi;
+}
+
+struct BatchRows {
+    const uint32_t* list;
+    const unsigned long long* n_a;  // rows of the list (or its first part)
+    const unsigned long long* n_b;  // second part (or nullptr)
+    uint32_t* next;                 // dynamic row counter of CTA classes
+};
+
+// ---- project, single pass (rows of many queries; contexts in shared memory)
+__global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, BatchRows L, uint32_t bitmap_words) {
+    extern __shared__ uint32_t bm[];
+    __shared__ uint32_t s_row, s_x, s_q;
+    __shared__ RowCtx s_c;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    uint32_t* stage = bm + bitmap_words + wib * kStage;
+    const uint32_t nrows = (uint32_t)(*L.n_a + *L.n_b);
+    for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
+        if (threadIdx.x == 0) {
+            uint32_t x;
+            s_q = query_of_row(Q, L.list[ri], &x);
+            s_x = x;
+            s_c = Q.rc[s_q];
+        }
+        __syncthreads();
+        const RowCtx& c = s_c;
+        const uint32_t x = s_x;
+        StageSink sink{stage, c.out, Q.rs[s_q], c.id2x[x]};
+        for (uint32_t t = 0; t < c.T; t++) {
+            const uint32_t lo = t * c.tile_width;
+            const uint32_t width = min(c.tile_width, c.m - lo);
+            const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
+            uint4* b4 = reinterpret_cast<uint4*>(bm);
+            for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            TileBitmap set{bm, lo};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
+            __syncthreads();
+        }
+        sink.flush();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_row, s_x, s_q;
+    __shared__ RowCtx s_c;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    uint32_t* stage = smem + (1u << block_lg) + wib * kStage;
+    const uint32_t nrows = (uint32_t)*L.n_a;
+    for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
+        if (threadIdx.x == 0) {
+            uint32_t x;
+            s_q = query_of_row(Q, L.list[ri], &x);
+            s_x = x;
+            s_c = Q.rc[s_q];
+        }
+        __syncthreads();
+        const RowCtx& c = s_c;
+        const uint32_t x = s_x;
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+        uint4* t4 = reinterpret_cast<uint4*>(smem);
+        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
+            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
+        __syncthreads();
+        HashSet set{smem, lg, c.err};
+        StageSink sink{stage, c.out, Q.rs[s_q], c.id2x[x]};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        sink.flush();
+    }
+}
+
+// Warp class: at most 8 warps per CTA, one context slot each.
+__global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ RowCtx s_c[8];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
+    uint32_t* stage = tab + (1u << warp_lg);
+    const uint32_t nrows = (uint32_t)*L.n_a;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
+        uint32_t x, qi = 0;
+        if (lane == 0) {
+            qi = query_of_row(Q, L.list[ri], &x);
+            s_c[wib] = Q.rc[qi];
+        }
+        qi = __shfl_sync(0xffffffffu, qi, 0);
+        x = __shfl_sync(0xffffffffu, x, 0);
+        __syncwarp();
+        const RowCtx& c = s_c[wib];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
+        for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
+        __syncwarp();
+        HashSet set{tab, lg, c.err};
+        StageSink sink{stage, c.out, Q.rs[qi], c.id2x[x]};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+        sink.flush();
+        __syncwarp();
+    }
+}
+
+// ---- COUNT, single pass: rows reserve output ranges from their query's
+// cursor, one atomic per 32 emitted groups.
+__device__ __forceinline__ void emit_groups(const RowCtx& c, const Reserve& rs, unsigned long long* out_cnt,
+                                            bool have, uint32_t xv, uint32_t zv, uint32_t cnt) {
+    const uint32_t b = __ballot_sync(0xffffffffu, have);
+    if (!b) return;
+    unsigned long long base = 0;
+    if (lane_id() == 0) base = atomicAdd(rs.cursor, (unsigned long long)__popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (have) {
+        const unsigned long long pos = base + __popc(b & lanemask_lt());
+        if (pos < rs.cap) {
+            c.out[pos] = make_uint2(xv, zv);
+            out_cnt[pos] = cnt;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ RowCtx s_c[8];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    uint32_t* keys = smem + ((size_t)wib << (warp_lg + 1));
+    uint32_t* vals = keys + (1u << warp_lg);
+    const uint32_t nrows = (uint32_t)*L.n_a;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
+        uint32_t x, qi = 0;
+        if (lane == 0) {
+            qi = query_of_row(Q, L.list[ri], &x);
+            s_c[wib] = Q.rc[qi];
+        }
+        qi = __shfl_sync(0xffffffffu, qi, 0);
+        x = __shfl_sync(0xffffffffu, x, 0);
+        __syncwarp();
+        const RowCtx& c = s_c[wib];
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
+        for (uint32_t s = lane; s < (1u << lg); s += 32) {
+            keys[s] = kEmpty32;
+            vals[s] = 0;
+        }
+        __syncwarp();
+        CountMap set{keys, vals, lg, c.err};
+        NullSink sink;
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+        __syncwarp();
+        const Reserve rs = Q.rs[qi];
+        const uint32_t xv = c.id2x[x];
+        unsigned long long* oc = Q.qin[qi].out_cnt;
+        for (uint32_t sb = 0; sb < (1u << lg); sb += 32) {
+            const uint32_t key = keys[sb + lane];
+            const bool have = key != kEmpty32;
+            emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[key]) : 0u, have ? vals[sb + lane] : 0u);
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_b_agg_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_row, s_x, s_q;
+    __shared__ RowCtx s_c;
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t nw_lg = 31 - __clz(nw);
+    uint32_t* keys = smem;
+    uint32_t* vals = smem + (1u << block_lg);
+    const uint32_t nrows = (uint32_t)*L.n_a;
+    for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
+        if (threadIdx.x == 0) {
+            uint32_t x;
+            s_q = query_of_row(Q, L.list[ri], &x);
+            s_x = x;
+            s_c = Q.rc[s_q];
+        }
+        __syncthreads();
+        const RowCtx& c = s_c;
+        const uint32_t x = s_x;
+        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+        for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
+            keys[s] = kEmpty32;
+            vals[s] = 0;
+        }
+        __syncthreads();
+        CountMap set{keys, vals, lg, c.err};
+        NullSink sink;
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        __syncthreads();
+        const Reserve rs = Q.rs[s_q];
+        const uint32_t xv = c.id2x[x];
+        unsigned long long* oc = Q.qin[s_q].out_cnt;
+        for (uint32_t sb = wib * 32; sb < (1u << lg); sb += nw * 32) {
+            const uint32_t key = keys[sb + lane];
+            const bool have = key != kEmpty32;
+            emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[key]) : 0u, have ? vals[sb + lane] : 0u);
+        }
+    }
+}
+
+// Classes 3/4 of COUNT: one CTA per row with a private counter array over
+// one z tile in global memory (L2-resident), plus a list of the z touched
+// in the tile, so emission and reset cost O(distinct z).
+struct TouchCountTile {
+    uint32_t* ctr;
+    uint32_t* touched;
+    uint32_t* n_touched;  // shared
+    uint32_t lo;
+    __device__ __forceinline__ bool insert(uint32_t z, bool act) {
+        if (act) {
+            const uint32_t zl = z - lo;
+            if (atomicAdd(&ctr[zl], 1u) == 0) touched[atomicAdd(n_touched, 1u)] = zl;
+        }
+        return false;
+    }
+};
+
+__global__ void __launch_bounds__(512) k_b_agg_tile(QueryPools Q, BatchRows L, uint32_t* scratch, uint32_t tile_cap) {
+    __shared__ uint32_t s_row, s_x, s_q, s_nt;
+    __shared__ RowCtx s_c;
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t nw_lg = 31 - __clz(nw);
+    uint32_t* ctr = scratch + (size_t)blockIdx.x * 2 * tile_cap;
+    uint32_t* touched = ctr + tile_cap;
+    const uint32_t nrows = (uint32_t)(*L.n_a + *L.n_b);
+    for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
+        if (threadIdx.x == 0) {
+            uint32_t x;
+            s_q = query_of_row(Q, L.list[ri], &x);
+            s_x = x;
+            s_c = Q.rc[s_q];
+        }
+        __syncthreads();
+        const RowCtx& c = s_c;
+        const uint32_t x = s_x;
+        const Reserve rs = Q.rs[s_q];
+        const uint32_t xv = c.id2x[x];
+        unsigned long long* oc = Q.qin[s_q].out_cnt;
+        for (uint32_t t = 0; t < c.T; t++) {
+            const uint32_t lo = t * c.tile_width;
+            if (threadIdx.x == 0) s_nt = 0;
+            __syncthreads();
+            TouchCountTile set{ctr, touched, &s_nt, lo};
+            NullSink sink;
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
+            __threadfence_block();
+            __syncthreads();
+            const uint32_t nt = s_nt;
+            for (uint32_t jb = wib * 32; jb < nt; jb += nw * 32) {
+                const uint32_t j = jb + lane;
+                const bool have = j < nt;
+                uint32_t zl = 0, v = 0;
+                if (have) {
+                    zl = __ldcg(&touched[j]);
+                    v = __ldcg(&ctr[zl]);
+                    ctr[zl] = 0;
+                }
+                emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[lo + zl]) : 0u, v);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace dim3g

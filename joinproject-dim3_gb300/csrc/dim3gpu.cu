@@ -85,6 +85,8 @@ struct Scalars {
     unsigned long long nx, ny, nz, nkept, total, outj;
     unsigned long long cursor;     // single-pass output cursor
     unsigned long long nrows[5];   // rows per class (index = class)
+    unsigned long long outj_cls[5];  // candidates per class (index = class)
+    unsigned long long cursor_at[3]; // single-pass cursor after the bitmap / block / warp kernel
     unsigned int err;
     unsigned int next_row[4];      // dynamic row counters of the CTA classes
     unsigned int pad;
@@ -350,7 +352,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     const uint32_t cap_w = 1u << (c->prm.warp_lg - 1);
     const uint32_t cap_b = 1u << (c->prm.block_lg - 1);
     k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, ucap, cls,
-                                                                &sc->outj);
+                                                                &sc->outj, sc->outj_cls);
     CHECK_LAUNCH();
     uint32_t* list_w = lists;
     uint32_t* list_b = lists + n;
@@ -395,10 +397,12 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
                                                                                          bm_words);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[5], st));
+        CU(cudaMemcpyAsync(&sc->cursor_at[0], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
         k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(rc, rs, L.b, L.nb,
                                                                                           c->prm.block_lg);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[6], st));
+        CU(cudaMemcpyAsync(&sc->cursor_at[1], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
         k_single_warp<<<resident_grid(k_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(rc, rs, L.w, L.nw,
                                                                                            c->prm.warp_lg);
         CHECK_LAUNCH();
@@ -409,10 +413,16 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in single pass (flags %u)", c->h_sc->err);
         const uint64_t total = c->h_sc->cursor;
         S.out_j = c->h_sc->outj;
+        S.n_out_cls[0] = c->h_sc->cursor_at[0];
+        S.n_out_cls[1] = c->h_sc->cursor_at[1] - c->h_sc->cursor_at[0];
+        S.n_out_cls[2] = total - c->h_sc->cursor_at[1];
         S.n_out = total;
         S.rows_warp = (uint32_t)c->h_sc->nrows[1];
         S.rows_block = (uint32_t)c->h_sc->nrows[2];
         S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
+        S.out_j_cls[0] = c->h_sc->outj_cls[3] + c->h_sc->outj_cls[4];
+        S.out_j_cls[1] = c->h_sc->outj_cls[2];
+        S.out_j_cls[2] = c->h_sc->outj_cls[1];
         *n_out = total;
         float a, b, e;
         cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
@@ -452,6 +462,9 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     S.rows_warp = (uint32_t)c->h_sc->nrows[1];
     S.rows_block = (uint32_t)c->h_sc->nrows[2];
     S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
+    S.out_j_cls[0] = c->h_sc->outj_cls[3] + c->h_sc->outj_cls[4];
+    S.out_j_cls[1] = c->h_sc->outj_cls[2];
+    S.out_j_cls[2] = c->h_sc->outj_cls[1];
     *n_out = total;
     if (jp.count_only) {
         float a, b, d;

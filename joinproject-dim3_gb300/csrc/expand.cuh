@@ -341,11 +341,12 @@ __global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uint32_t* 
 // (join-aggregate, 32-bit per-group counters) a row of 2^32 or more
 // candidates raises kErrCountRange.
 __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range,
-                           uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj) {
+                           uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj,
+                           unsigned long long* outj_cls) {
     const uint32_t lane = lane_id();
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long acc = 0;
+    unsigned long long acc = 0, acc_cls[5] = {0, 0, 0, 0, 0};
     for (uint64_t x = gw; x < n; x += nwarps) {
         uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
         unsigned long long w = 0;
@@ -357,12 +358,20 @@ __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b,
         if (lane == 0) {
             uint32_t u = (uint32_t)(w < c.m ? w : c.m);
             ucap[x] = u;
-            cls[x] = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
+            const uint32_t k = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
+            cls[x] = (uint8_t)k;
             if (check_range && w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
             acc += w;
+#pragma unroll
+            for (uint32_t j = 1; j < 5; j++) acc_cls[j] += (j == k) ? w : 0ull;
         }
     }
-    if (lane == 0 && acc) atomicAdd(outj, acc);
+    if (lane == 0 && acc) {
+        atomicAdd(outj, acc);
+#pragma unroll
+        for (uint32_t j = 1; j < 5; j++)
+            if (acc_cls[j]) atomicAdd(&outj_cls[j], acc_cls[j]);
+    }
 }
 
 struct ClassSrc {

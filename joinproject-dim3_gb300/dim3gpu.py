@@ -45,13 +45,18 @@ class Stats(ctypes.Structure):
         ("ms_map", ctypes.c_float), ("ms_csr", ctypes.c_float), ("ms_count", ctypes.c_float),
         ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float), ("launches", ctypes.c_uint64),
         ("ms_count_cls", ctypes.c_float * 3), ("ms_write_cls", ctypes.c_float * 3),
+        ("out_j_cls", ctypes.c_uint64 * 3), ("n_out_cls", ctypes.c_uint64 * 3),
     ]
 
     def as_dict(self):
         d = {}
         for k, _ in self._fields_:
             v = getattr(self, k)
-            d[k] = [round(float(x), 3) for x in v] if k.endswith("_cls") else v
+            if k.startswith("ms_") and k.endswith("_cls"):
+                v = [round(float(x), 3) for x in v]
+            elif k.endswith("_cls"):
+                v = [int(x) for x in v]
+            d[k] = v
         return d
 
 
