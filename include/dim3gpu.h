@@ -133,6 +133,67 @@ int dim3g_join_count_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, co
 int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
                                uint32_t* d_out, uint64_t capacity, uint64_t* n_out, void* cuda_stream);
 
+/* ---- resident relation sets and many-query passes ---------------------
+ * No counterpart in the reference, whose entry points take one join at a
+ * time.  A relation set builds on the GPU, for all its relations in one
+ * pass, each relation's value -> id maps and both CSR forms (the relation
+ * as R, grouped by its first column; as S, grouped by its y column) and
+ * keeps them in device memory.  A join of two relations of a set then skips
+ * hashing and CSR construction: it costs a y-id translation and the
+ * expansion.  dim3g_relset_join runs many such joins in one pass, the rows
+ * of all queries sharing the row kernels.
+ * Per query the result set is that of dim3g_join_project_device (R =
+ * relation r, S = relation s; the larger relation drives the rows, so a
+ * smaller R yields (z, x) pairs and `swapped` = 1) or, for DIM3G_OP_COUNT,
+ * that of dim3g_join_count_device; pairs and groups come in unspecified
+ * order. */
+typedef struct dim3g_relset dim3g_relset;
+typedef struct {
+    const uint32_t* d_pairs; /* device (first, y) pairs, 8-byte aligned */
+    uint64_t n;              /* tuples */
+} dim3g_relation;
+#define DIM3G_OP_PROJECT 0
+#define DIM3G_OP_COUNT 1
+typedef struct {
+    uint32_t r, s;     /* relation indices: R(x, y), S(z, y) */
+    uint32_t op;       /* DIM3G_OP_PROJECT or DIM3G_OP_COUNT */
+    uint32_t swapped;  /* out: 1 when the pairs are (z, x) */
+    uint32_t* d_out;   /* device pairs, `capacity` of them */
+    uint64_t* d_cnt;   /* device counts, `capacity` of them (DIM3G_OP_COUNT) */
+    uint64_t capacity;
+    uint64_t n_out;    /* out: distinct pairs; on DIM3G_ERR_CAPACITY the pairs needed */
+    uint64_t out_j;    /* out: joining tuple pairs (candidates) */
+    int32_t status;    /* out: DIM3G_OK, DIM3G_ERR_CAPACITY or DIM3G_ERR_DEVICE */
+    uint32_t pad;
+} dim3g_query;
+/* Builds the indexes of n relations; synchronous.  The pair arrays must stay
+ * valid and unchanged while the set lives.  Limit: fewer than 2^32-1 tuples
+ * in the whole set. */
+int dim3g_relset_create(dim3g_ctx* ctx, const dim3g_relation* rels, uint32_t n, dim3g_relset** set);
+void dim3g_relset_destroy(dim3g_relset* set);
+/* Device bytes the set holds (indexes and query scratch). */
+uint64_t dim3g_relset_bytes(const dim3g_relset* set);
+/* Runs n queries over the set in one pass on the context's stream;
+ * synchronous.  Each query gets its own status; the call returns DIM3G_OK
+ * when all are DIM3G_OK, else the first failing status. */
+int dim3g_relset_join(dim3g_relset* set, dim3g_query* q, uint32_t n);
+
+/* ---- batches of independent joins, one CUDA graph --------------------
+ * n joins, each with its own device R (rels[2i]) and S (rels[2i+1]),
+ * planned once: the index build of all 2n relations and the query pass are
+ * captured into one CUDA graph, and every dim3g_batch_run is one graph
+ * launch (no host synchronisation inside).  q[i].r / q[i].s are ignored;
+ * outputs, capacities and ops are fixed at creation.  The inputs may change
+ * between runs (not their sizes).  Results land in q[i] on every run. */
+typedef struct dim3g_batch dim3g_batch;
+int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_query* q, uint32_t n,
+                       dim3g_batch** b);
+int dim3g_batch_run(dim3g_batch* b, dim3g_query* q);
+/* Device ms of the last run (graph launch to completion), kernel launches
+ * per run, device bytes held. */
+int dim3g_batch_info(const dim3g_batch* b, float* ms_last, uint64_t* launches_per_run, uint64_t* device_bytes);
+void dim3g_batch_destroy(dim3g_batch* b);
+
 /* ---- L+S mapper -----------------------------------------------------
  * Replaces LS_mapper<T,H,Tcounter> (Include/L+S_mapper.hpp:11-160): a GPU
  * value -> dense id map.  insert() gives every key its existing id or the

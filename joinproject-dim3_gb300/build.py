@@ -3,7 +3,9 @@
     libdim3gpu.so  CUDA kernels + C ABI (nvcc, sm_103a only)
     libdim3gen.so  seeded workload generators (gcc, OpenMP)
 
-Both are written next to this file; `python build.py` builds them.
+The CUDA translation units compile in parallel to objects under _build/,
+then link into one shared library.  Both libraries are written next to this
+file; `python build.py` builds them.
 """
 import os
 import subprocess
@@ -12,11 +14,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
 GPU_SO = os.path.join(HERE, "libdim3gpu.so")
 GEN_SO = os.path.join(HERE, "libdim3gen.so")
+GPU_TUS = ["dim3gpu.cu", "batch.cu", "noalloc.cu"]
 
-NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-shared"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC"]
 
 
 def _nvcc():
@@ -37,17 +41,27 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _obj(tu):
+    return os.path.join(OBJ, tu.replace(".cu", ".o"))
+
+
 def commands(force=False):
-    cmds = []
-    gpu_deps = _sources(".cu") + _sources(".cuh") + [os.path.join(REPO, "include", "dim3gpu.h")]
-    if force or _stale(GPU_SO, gpu_deps):
-        cmds.append([_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "dim3gpu.cu"), os.path.join(CSRC, "noalloc.cu"),
-                                              "-o", GPU_SO])
+    """Two stages: [compile commands], [link commands]."""
+    compile_cmds, link_cmds = [], []
+    headers = _sources(".cuh") + _sources(".h") + [os.path.join(REPO, "include", "dim3gpu.h")]
+    objs = []
+    for tu in GPU_TUS:
+        src, obj = os.path.join(CSRC, tu), _obj(tu)
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            compile_cmds.append([_nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj])
+    if force or compile_cmds or _stale(GPU_SO, objs):
+        link_cmds.append([_nvcc()] + ARCH + ["-shared"] + objs + ["-o", GPU_SO])
     gen_deps = [os.path.join(CSRC, "dim3gen.c"), os.path.join(CSRC, "dim3gen.h")]
     if force or _stale(GEN_SO, gen_deps):
-        cmds.append(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-                     os.path.join(CSRC, "dim3gen.c"), "-o", GEN_SO])
-    return cmds
+        compile_cmds.append(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
+                             os.path.join(CSRC, "dim3gen.c"), "-o", GEN_SO])
+    return compile_cmds, link_cmds
 
 
 def run_parallel(cmds):
@@ -63,7 +77,10 @@ def run_parallel(cmds):
 
 
 def build(force=False):
-    run_parallel(commands(force))
+    os.makedirs(OBJ, exist_ok=True)
+    compile_cmds, link_cmds = commands(force)
+    run_parallel(compile_cmds)
+    run_parallel(link_cmds)
     return GPU_SO, GEN_SO
 
 

@@ -99,8 +99,48 @@ __device__ __forceinline__ void emit_map_slots_warp(const RowCtx& c, AggOut ao, 
     }
 }
 
+// A map-class row counts with one counter per z of the whole domain instead
+// of a z -> count hash map when the m counters fit the kernel's map memory
+// (2^words_lg words) and scanning them costs little against the row's
+// candidates (m <= 8 u).
+__device__ __forceinline__ bool use_row_counters(uint32_t m, uint32_t u, uint32_t words_lg) {
+    return (uint64_t)m <= (1ull << words_lg) && (uint64_t)m <= 8ull * u;
+}
+
+// Warp-collective emission of the nonzero direct counters ctr[s0, s1): the
+// counter index is the z id.  shared_pos / local_pos as above.
+__device__ __forceinline__ void emit_counters_warp(const RowCtx& c, AggOut ao, const uint32_t* ctr, uint32_t s0,
+                                                   uint32_t s1, uint32_t xv, unsigned long long base, uint32_t lim,
+                                                   uint32_t* shared_pos, uint32_t* local_pos) {
+    const uint32_t lane = lane_id();
+    for (uint32_t sb = s0; sb < s1; sb += 32) {
+        const uint32_t s = sb + lane;
+        const uint32_t v = (s < s1) ? ctr[s] : 0u;
+        const uint32_t b = __ballot_sync(0xffffffffu, v != 0);
+        if (!b) continue;
+        uint32_t pb;
+        if (shared_pos) {
+            pb = 0;
+            if (lane == 0) pb = atomicAdd(shared_pos, (uint32_t)__popc(b));
+            pb = __shfl_sync(0xffffffffu, pb, 0);
+        } else {
+            pb = *local_pos;
+            *local_pos += __popc(b);
+        }
+        if (v) {
+            const uint32_t pos = pb + __popc(b & lanemask_lt());
+            if (pos < lim) {
+                c.out[base + pos] = make_uint2(xv, __ldg(&c.id2z[s]));
+                ao.cnt[base + pos] = v;
+            } else {
+                raise_error(c.err, kErrOutputBound);
+            }
+        }
+    }
+}
+
 // Class 1 write pass: one warp per row; per warp 2^lg keys + 2^lg counts.
-__global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
                                                   const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
@@ -109,7 +149,20 @@ __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uin
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        NullSink sink;
+        uint32_t pos = 0;
+        if (use_row_counters(c.m, u, warp_lg + 1)) {
+            for (uint32_t s = lane; s < c.m; s += 32) keys[s] = 0;  // keys + vals: one counter array
+            __syncwarp();
+            CountTile set{keys, 0};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+            __syncwarp();
+            emit_counters_warp(c, ao, keys, 0, c.m, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+            __syncwarp();
+            continue;
+        }
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
         for (uint32_t s = lane; s < (1u << lg); s += 32) {
             keys[s] = kEmpty32;
@@ -117,17 +170,15 @@ __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, const uin
         }
         __syncwarp();
         CountMap set{keys, vals, lg, c.err};
-        NullSink sink;
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
         __syncwarp();
-        uint32_t pos = 0;
         emit_map_slots_warp(c, ao, keys, vals, 0, 1u << lg, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
         __syncwarp();
     }
 }
 
 // Class 2 write pass: one CTA per row.
-__global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
                                                    const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_pos, s_row;
@@ -138,27 +189,39 @@ __global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, const ui
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        const bool direct = use_row_counters(c.m, u, block_lg + 1);
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
-        for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
-            keys[s] = kEmpty32;
-            vals[s] = 0;
+        if (direct) {
+            for (uint32_t s = threadIdx.x; s < c.m; s += blockDim.x) keys[s] = 0;
+        } else {
+            for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
+                keys[s] = kEmpty32;
+                vals[s] = 0;
+            }
         }
         if (threadIdx.x == 0) s_pos = 0;
         __syncthreads();
-        CountMap set{keys, vals, lg, c.err};
         NullSink sink;
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        if (direct) {
+            CountTile set{keys, 0};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        } else {
+            CountMap set{keys, vals, lg, c.err};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        }
         __syncthreads();
-        const uint32_t span = (1u << lg);
-        const uint32_t per = (span + nw - 1) / nw;
+        const uint32_t span = direct ? c.m : (1u << lg);
+        const uint32_t per = (((span + nw - 1) / nw) + 31) & ~31u;
         const uint32_t s0 = min(span, wib * per), s1 = min(span, s0 + per);
-        emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        if (direct) emit_counters_warp(c, ao, keys, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        else emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
     }
 }
 
 // Classes 3/4 write pass: one CTA per row; a counter per z of one tile.
-__global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, const uint32_t* __restrict__ rows,
                                                    const unsigned long long* __restrict__ n3,
                                                    const unsigned long long* __restrict__ n4) {
     extern __shared__ uint32_t ctr[];

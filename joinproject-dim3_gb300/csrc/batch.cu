@@ -1,0 +1,723 @@
+// batch.cu -- resident relation sets, many-query passes, and batches of
+// independent joins run as one CUDA graph (host side; kernels in batch.cuh).
+//
+// Relation set build (one stream, no host synchronisation inside):
+//   memsets -> k_ix_insert -> k_ix_layout -> id scans (TF, TY) -> k_ix_map
+//   -> CSR scans (by f, by (y, f tile)) -> k_ix_scatter
+// Query pass over queries (P, Q) of a set:
+//   k_q_setup -> k_q_ymap -> k_q_entries -> k_q_rows -> k_q_row_work
+//   -> class lists (prefix sums) -> project row kernels -> COUNT row kernels
+//   -> per-query results to pinned host memory
+// Every size the launches depend on is known on the host from the tuple
+// counts; counts that depend on the data (distinct values, rows per class,
+// output sizes) stay on the device.  The one data-dependent bound, the
+// (y, f tile) key space, is checked on the device; on overflow the host
+// regrows that pool and runs again.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/dim3gpu.h"
+#include "batch.cuh"
+#include "internal.h"
+#include "scan.cuh"
+
+using namespace dim3g;
+namespace I = dim3g_internal;
+
+namespace {
+
+#define BCU(call)                                                                                             \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess) return I::fail(ctx, DIM3G_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+#define BLAUNCH()                          \
+    do {                                   \
+        BCU(cudaGetLastError());           \
+        launches++;                        \
+    } while (0)
+
+uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Offsets of typed arrays inside one device allocation.
+struct Layout {
+    size_t total = 0;
+    template <class T>
+    size_t add(uint64_t count) {
+        size_t o = total;
+        total += align256((size_t)(count ? count : 1) * sizeof(T));
+        return o;
+    }
+};
+
+template <class K>
+unsigned resident(K kernel, int block, size_t smem, int sm) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        per = 1;
+    }
+    return (unsigned)(per * sm);
+}
+unsigned elem_grid(uint64_t n, int sm) {
+    uint64_t b = (n + 255) / 256;
+    uint64_t cap = (uint64_t)sm * 8;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+struct Tuning {
+    uint32_t warp_lg, block_lg, block_threads, tile_lg;
+};
+Tuning tuning_of(const dim3g_ctx* ctx) {
+    int64_t w = 11, b = 14, t = 512, tl = 19;
+    dim3g_get_param(ctx, "warp_slots_log2", &w);
+    dim3g_get_param(ctx, "block_slots_log2", &b);
+    dim3g_get_param(ctx, "block_threads", &t);
+    dim3g_get_param(ctx, "tile_bits_log2", &tl);
+    if (tl > 19) tl = 19;  // the batch bitmap kernel runs 512-thread CTAs
+    return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl};
+}
+
+// Warps per CTA of the warp-class kernels (about half an SM's shared memory).
+uint32_t warps_for(size_t per_warp) {
+    size_t w = (size_t)112 * 1024 / per_warp;
+    return (uint32_t)(w < 1 ? 1 : (w > 8 ? 8 : w));
+}
+
+}  // namespace
+
+// ============================================================ relation set
+struct dim3g_relset {
+    dim3g_ctx* ctx = nullptr;
+    uint32_t nrel = 0;
+    std::vector<RelIn> h_in;
+    std::vector<uint64_t> h_tup_off, h_tab_off;
+    uint64_t ntot = 0, tabtot = 0, yt_cap = 0;
+    uint32_t tile_lg = 19;
+    char* mem = nullptr;
+    size_t mem_bytes = 0;
+    RelPools P{};
+    uint64_t* bsum = nullptr;
+    uint64_t bsum_n = 0;
+    // query pass scratch (grow-only)
+    char* qmem = nullptr;
+    size_t qmem_bytes = 0;
+    uint32_t* agg_scratch = nullptr;
+    size_t agg_bytes = 0;
+    QueryRes* h_res = nullptr;  // pinned
+    uint32_t h_res_n = 0;
+    unsigned long long* h_need = nullptr;  // pinned: yt keys needed, err
+    uint64_t launches_build = 0;
+
+    ~dim3g_relset() {
+        if (mem) cudaFree(mem);
+        if (qmem) cudaFree(qmem);
+        if (agg_scratch) cudaFree(agg_scratch);
+        if (h_res) cudaFreeHost(h_res);
+        if (h_need) cudaFreeHost(h_need);
+    }
+};
+
+namespace {
+
+// Host layout of a relation set from its tuple counts.
+int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_t yt_cap) {
+    dim3g_ctx* ctx = s->ctx;
+    s->nrel = n;
+    s->h_in.resize(n);
+    s->h_tup_off.assign(n + 1, 0);
+    s->h_tab_off.assign(n + 1, 0);
+    uint64_t yt_guess = 1;
+    for (uint32_t r = 0; r < n; r++) {
+        if (!rels[r].d_pairs && rels[r].n) return I::fail(ctx, DIM3G_ERR_INVALID, "relation %u: null pairs", r);
+        if ((uintptr_t)rels[r].d_pairs & 7u) return I::fail(ctx, DIM3G_ERR_INVALID, "relation %u: pairs not 8-byte aligned", r);
+        s->h_in[r] = RelIn{(const uint2*)rels[r].d_pairs, rels[r].n};
+        s->h_tup_off[r + 1] = s->h_tup_off[r] + rels[r].n;
+        const uint64_t cap = next_pow2(rels[r].n * 2 < 1024 ? 1024 : rels[r].n * 2);
+        s->h_tab_off[r + 1] = s->h_tab_off[r] + cap;
+        yt_guess += 2 * rels[r].n + 2;
+    }
+    s->ntot = s->h_tup_off[n];
+    if (s->ntot >= 0xFFFFFFFFull)
+        return I::fail(ctx, DIM3G_ERR_UNSUPPORTED, "a relation set holds fewer than 2^32-1 tuples in total");
+    s->tabtot = s->h_tab_off[n];
+    s->yt_cap = yt_cap ? yt_cap : yt_guess;
+
+    Layout L;
+    const size_t o_in = L.add<RelIn>(n), o_rel = L.add<RelDev>(n), o_tup = L.add<uint64_t>(n + 1),
+                 o_tab = L.add<uint64_t>(n + 1), o_TF = L.add<unsigned long long>(s->tabtot),
+                 o_TY = L.add<unsigned long long>(s->tabtot), o_nf = L.add<unsigned long long>(n),
+                 o_ny = L.add<unsigned long long>(n), o_id2f = L.add<uint32_t>(s->ntot),
+                 o_id2y = L.add<uint32_t>(s->ntot), o_Pm = L.add<uint2>(s->ntot), o_deg = L.add<uint32_t>(s->ntot + 1),
+                 o_JRf = L.add<uint32_t>(s->ntot + 1), o_curF = L.add<uint32_t>(s->ntot + 1),
+                 o_ICf = L.add<uint32_t>(s->ntot), o_ICr = L.add<uint32_t>(s->ntot), o_cyt = L.add<uint32_t>(s->yt_cap),
+                 o_JRy = L.add<uint32_t>(s->yt_cap), o_curY = L.add<uint32_t>(s->yt_cap),
+                 o_ICy = L.add<uint32_t>(s->ntot), o_VSy = L.add<uint32_t>(s->ntot), o_err = L.add<uint32_t>(4),
+                 o_need = L.add<unsigned long long>(2);
+    uint64_t sn = scan_storage(s->tabtot);
+    const uint64_t s2 = scan_storage(s->ntot + 1), s3 = scan_storage(s->yt_cap);
+    if (s2 > sn) sn = s2;
+    if (s3 > sn) sn = s3;
+    const size_t o_bsum = L.add<uint64_t>(sn);
+    if (s->mem && s->mem_bytes < L.total) {
+        cudaFree(s->mem);
+        s->mem = nullptr;
+        s->mem_bytes = 0;
+    }
+    if (!s->mem) {
+        if (cudaMalloc(&s->mem, L.total) != cudaSuccess) {
+            cudaGetLastError();
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "relation set: device allocation of %zu bytes failed", L.total);
+        }
+        s->mem_bytes = L.total;
+    }
+    char* m = s->mem;
+    RelPools& P = s->P;
+    P.in = (const RelIn*)(m + o_in);
+    P.rel = (RelDev*)(m + o_rel);
+    P.tup_off = (const uint64_t*)(m + o_tup);
+    P.tab_off = (const uint64_t*)(m + o_tab);
+    P.nrel = n;
+    P.ntot = s->ntot;
+    P.TF = (unsigned long long*)(m + o_TF);
+    P.TY = (unsigned long long*)(m + o_TY);
+    P.nf_cnt = (unsigned long long*)(m + o_nf);
+    P.ny_cnt = (unsigned long long*)(m + o_ny);
+    P.id2f = (uint32_t*)(m + o_id2f);
+    P.id2y = (uint32_t*)(m + o_id2y);
+    P.Pm = (uint2*)(m + o_Pm);
+    P.degF = (uint32_t*)(m + o_deg);
+    P.JRf = (uint32_t*)(m + o_JRf);
+    P.curF = (uint32_t*)(m + o_curF);
+    P.ICf = (uint32_t*)(m + o_ICf);
+    P.ICr = (uint32_t*)(m + o_ICr);
+    P.cnt_yt = (uint32_t*)(m + o_cyt);
+    P.JRy = (uint32_t*)(m + o_JRy);
+    P.curY = (uint32_t*)(m + o_curY);
+    P.yt_cap = s->yt_cap;
+    P.ICy = (uint32_t*)(m + o_ICy);
+    P.VSy = (uint32_t*)(m + o_VSy);
+    P.err = (uint32_t*)(m + o_err);
+    P.yt_need = (unsigned long long*)(m + o_need);
+    s->bsum = (uint64_t*)(m + o_bsum);
+    s->bsum_n = sn;
+    BCU(cudaMemcpy((void*)P.in, s->h_in.data(), n * sizeof(RelIn), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy((void*)P.tup_off, s->h_tup_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy((void*)P.tab_off, s->h_tab_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+    return DIM3G_OK;
+}
+
+// The build launches (stream ordered; capturable).
+int relset_enqueue_build(dim3g_relset* s, cudaStream_t st, uint64_t& launches) {
+    dim3g_ctx* ctx = s->ctx;
+    const RelPools& P = s->P;
+    const int sm = I::sm_count(ctx);
+    BCU(cudaMemsetAsync(P.TF, 0xff, s->tabtot * 8, st));
+    BCU(cudaMemsetAsync(P.TY, 0xff, s->tabtot * 8, st));
+    BCU(cudaMemsetAsync(P.nf_cnt, 0, s->nrel * 8, st));
+    BCU(cudaMemsetAsync(P.ny_cnt, 0, s->nrel * 8, st));
+    BCU(cudaMemsetAsync(P.degF, 0, (s->ntot + 1) * 4, st));
+    BCU(cudaMemsetAsync(P.cnt_yt, 0, s->yt_cap * 4, st));
+    BCU(cudaMemsetAsync(P.err, 0, 16, st));
+    if (s->ntot) {
+        k_ix_insert<<<elem_grid(s->ntot, sm), 256, 0, st>>>(P);
+        BLAUNCH();
+    }
+    k_ix_layout<<<1, 1024, 0, st>>>(P, s->tile_lg);
+    BLAUNCH();
+    device_scan(OccupiedSrc{P.TF}, AssignIdDst{P.TF, P.id2f}, s->tabtot, s->bsum, nullptr, st);
+    launches += scan_launches(s->tabtot);
+    device_scan(OccupiedSrc{P.TY}, AssignIdDst{P.TY, P.id2y}, s->tabtot, s->bsum, nullptr, st);
+    launches += scan_launches(s->tabtot);
+    BCU(cudaGetLastError());
+    if (s->ntot) {
+        k_ix_map<<<elem_grid(s->ntot, sm), 256, 0, st>>>(P);
+        BLAUNCH();
+    }
+    device_scan(U32Src{P.degF}, RowPtrDst{P.JRf, P.curF}, s->ntot + 1, s->bsum, nullptr, st);
+    launches += scan_launches(s->ntot + 1);
+    device_scan(U32Src{P.cnt_yt}, RowPtrDst{P.JRy, P.curY}, s->yt_cap, s->bsum, nullptr, st);
+    launches += scan_launches(s->yt_cap);
+    BCU(cudaGetLastError());
+    if (s->ntot) {
+        k_ix_scatter<<<elem_grid(s->ntot, sm), 256, 0, st>>>(P);
+        BLAUNCH();
+    }
+    BCU(cudaMemcpyAsync(s->h_need, P.yt_need, 8, cudaMemcpyDeviceToHost, st));
+    BCU(cudaMemcpyAsync(s->h_need + 1, P.err, 4, cudaMemcpyDeviceToHost, st));
+    return DIM3G_OK;
+}
+
+// ---------------------------------------------------------------- queries
+struct QueryPlan {
+    uint32_t nq = 0;
+    std::vector<QueryIn> h_qin;
+    std::vector<uint64_t> h_qt_off, h_qrow_off;
+    std::vector<uint32_t> swapped;
+    uint64_t ntot = 0, nrows = 0;
+    bool has_project = false, has_count = false;
+    QueryPools Q{};
+    uint32_t* lists = nullptr;             // 3 x nrows
+    unsigned long long* ncls = nullptr;    // rows per class 0..8
+    uint32_t* next_row = nullptr;          // 4 dynamic counters
+    uint64_t* bsum = nullptr;
+};
+
+int query_plan(dim3g_relset* s, const dim3g_query* q, uint32_t nq, QueryPlan& qp) {
+    dim3g_ctx* ctx = s->ctx;
+    qp.nq = nq;
+    qp.h_qin.resize(nq);
+    qp.swapped.resize(nq);
+    qp.h_qt_off.assign(nq + 1, 0);
+    qp.h_qrow_off.assign(nq + 1, 0);
+    for (uint32_t i = 0; i < nq; i++) {
+        if (q[i].r >= s->nrel || q[i].s >= s->nrel)
+            return I::fail(ctx, DIM3G_ERR_INVALID, "query %u: relation index out of range", i);
+        if (q[i].op != DIM3G_OP_PROJECT && q[i].op != DIM3G_OP_COUNT)
+            return I::fail(ctx, DIM3G_ERR_INVALID, "query %u: unknown op %u", i, q[i].op);
+        if (q[i].capacity && (!q[i].d_out || (q[i].op == DIM3G_OP_COUNT && !q[i].d_cnt)))
+            return I::fail(ctx, DIM3G_ERR_INVALID, "query %u: null output with nonzero capacity", i);
+        if (((uintptr_t)q[i].d_out & 7u) || ((uintptr_t)q[i].d_cnt & 7u))
+            return I::fail(ctx, DIM3G_ERR_INVALID, "query %u: outputs not 8-byte aligned", i);
+        const uint64_t nr = s->h_in[q[i].r].n, ns = s->h_in[q[i].s].n;
+        const bool sw = nr < ns;  // the larger relation drives the rows
+        QueryIn qi{};
+        qi.p = sw ? q[i].s : q[i].r;
+        qi.q = sw ? q[i].r : q[i].s;
+        qi.op = q[i].op == DIM3G_OP_COUNT ? kOpCount : kOpProject;
+        qi.out = (uint2*)q[i].d_out;
+        qi.out_cnt = (unsigned long long*)q[i].d_cnt;
+        qi.cap = q[i].capacity;
+        // an empty side gives an empty result: no rows
+        const uint64_t np = (nr == 0 || ns == 0) ? 0 : s->h_in[qi.p].n;
+        qp.h_qin[i] = qi;
+        qp.swapped[i] = sw;
+        qp.h_qt_off[i + 1] = qp.h_qt_off[i] + np;
+        qp.h_qrow_off[i + 1] = qp.h_qrow_off[i] + np + 1;
+        if (qi.op == kOpCount) qp.has_count = true;
+        else qp.has_project = true;
+    }
+    qp.ntot = qp.h_qt_off[nq];
+    qp.nrows = qp.h_qrow_off[nq];
+    if (qp.nrows >= 0xFFFFFFFFull)
+        return I::fail(ctx, DIM3G_ERR_UNSUPPORTED, "a query pass covers fewer than 2^32-1 rows in total");
+
+    Layout L;
+    const size_t o_qin = L.add<QueryIn>(nq), o_qt = L.add<uint64_t>(nq + 1), o_qr = L.add<uint64_t>(nq + 1),
+                 o_ymap = L.add<uint32_t>(qp.ntot), o_ICq = L.add<uint32_t>(qp.ntot), o_JRq = L.add<uint32_t>(qp.nrows),
+                 o_ucap = L.add<uint32_t>(qp.nrows), o_cls = L.add<uint8_t>(qp.nrows),
+                 o_wrow = L.add<unsigned long long>(qp.nrows), o_rc = L.add<RowCtx>(nq),
+                 o_rs = L.add<Reserve>(nq), o_res = L.add<QueryRes>(nq), o_lists = L.add<uint32_t>(3 * qp.nrows),
+                 o_ncls = L.add<unsigned long long>(16), o_next = L.add<uint32_t>(8),
+                 o_bsum = L.add<uint64_t>(scan_storage(qp.nrows));
+    if (s->qmem && s->qmem_bytes < L.total) {
+        cudaFree(s->qmem);
+        s->qmem = nullptr;
+        s->qmem_bytes = 0;
+    }
+    if (!s->qmem) {
+        if (cudaMalloc(&s->qmem, L.total) != cudaSuccess) {
+            cudaGetLastError();
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "query pass: device allocation of %zu bytes failed", L.total);
+        }
+        s->qmem_bytes = L.total;
+    }
+    if (s->h_res_n < nq) {
+        if (s->h_res) cudaFreeHost(s->h_res);
+        s->h_res = nullptr;
+        s->h_res_n = 0;
+        if (cudaMallocHost((void**)&s->h_res, (size_t)nq * sizeof(QueryRes)) != cudaSuccess) {
+            cudaGetLastError();
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "query pass: pinned allocation failed");
+        }
+        s->h_res_n = nq;
+    }
+    char* m = s->qmem;
+    QueryPools& Q = qp.Q;
+    const RelPools& P = s->P;
+    Q.rel = P.rel;
+    Q.qin = (const QueryIn*)(m + o_qin);
+    Q.nq = nq;
+    Q.qt_off = (const uint64_t*)(m + o_qt);
+    Q.qrow_off = (const uint64_t*)(m + o_qr);
+    Q.ntot = qp.ntot;
+    Q.nrows = qp.nrows;
+    Q.TY = P.TY;
+    Q.id2f = P.id2f;
+    Q.id2y = P.id2y;
+    Q.JRf = P.JRf;
+    Q.ICf = P.ICf;
+    Q.ICr = P.ICr;
+    Q.JRy = P.JRy;
+    Q.ICy = P.ICy;
+    Q.VSy = P.VSy;
+    Q.yt_need = P.yt_need;
+    Q.yt_cap = P.yt_cap;
+    Q.ymap = (uint32_t*)(m + o_ymap);
+    Q.ICq = (uint32_t*)(m + o_ICq);
+    Q.JRq = (uint32_t*)(m + o_JRq);
+    Q.ucap = (uint32_t*)(m + o_ucap);
+    Q.cls = (uint8_t*)(m + o_cls);
+    Q.wrow = (unsigned long long*)(m + o_wrow);
+    Q.rc = (RowCtx*)(m + o_rc);
+    Q.rs = (Reserve*)(m + o_rs);
+    Q.res = (QueryRes*)(m + o_res);
+    qp.lists = (uint32_t*)(m + o_lists);
+    qp.ncls = (unsigned long long*)(m + o_ncls);
+    qp.next_row = (uint32_t*)(m + o_next);
+    qp.bsum = (uint64_t*)(m + o_bsum);
+    return DIM3G_OK;
+}
+
+// Uploads the query descriptors (outside any capture: pageable copies).
+int query_upload(dim3g_relset* s, const QueryPlan& qp) {
+    dim3g_ctx* ctx = s->ctx;
+    BCU(cudaMemcpy((void*)qp.Q.qin, qp.h_qin.data(), qp.nq * sizeof(QueryIn), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy((void*)qp.Q.qt_off, qp.h_qt_off.data(), (qp.nq + 1) * 8, cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy((void*)qp.Q.qrow_off, qp.h_qrow_off.data(), (qp.nq + 1) * 8, cudaMemcpyHostToDevice));
+    return DIM3G_OK;
+}
+
+struct ClassList {
+    uint32_t* list;
+    unsigned long long* n;
+};
+
+// The query pass (stream ordered; capturable).
+int query_enqueue(dim3g_relset* s, QueryPlan& qp, cudaStream_t st, uint64_t& launches) {
+    dim3g_ctx* ctx = s->ctx;
+    QueryPools& Q = qp.Q;
+    const int sm = I::sm_count(ctx);
+    const Tuning tu = tuning_of(ctx);
+    const uint32_t nq = qp.nq;
+    BCU(cudaMemsetAsync(qp.ncls, 0, 16 * 8, st));
+    BCU(cudaMemsetAsync(Q.cls, 0, qp.nrows, st));
+    BCU(cudaMemsetAsync(Q.wrow, 0, qp.nrows * 8, st));
+    BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));
+    k_q_setup<<<(nq + 127) / 128, 128, 0, st>>>(Q);
+    BLAUNCH();
+    if (qp.ntot) {
+        k_q_ymap<<<elem_grid(qp.ntot, sm), 256, 0, st>>>(Q);
+        BLAUNCH();
+        k_q_entries<<<elem_grid(qp.ntot, sm), 256, 0, st>>>(Q);
+        BLAUNCH();
+    }
+    k_q_rows<<<elem_grid(qp.nrows, sm), 256, 0, st>>>(Q);
+    BLAUNCH();
+    const uint32_t cap_w = 1u << (tu.warp_lg - 1), cap_b = 1u << (tu.block_lg - 1);
+    k_q_row_work<<<elem_grid(qp.nrows, sm), 256, 0, st>>>(Q, cap_w, cap_b);
+    BLAUNCH();
+    uint32_t* lw = qp.lists;
+    uint32_t* lb = qp.lists + qp.nrows;
+    uint32_t* lm = qp.lists + 2 * qp.nrows;
+    const uint32_t bm_words = (1u << s->tile_lg) / 32;  // the tiling the set was built with
+    for (int op = 0; op < 2; op++) {
+        if (op == 0 && !qp.has_project) continue;
+        if (op == 1 && !qp.has_count) continue;
+        const uint8_t k0 = op ? 4 : 0;
+        unsigned long long* n = qp.ncls + 4 * op;  // n[1..4]: rows of classes k0+1..k0+4
+        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 1)}, ListDst{lw, nullptr}, qp.nrows, qp.bsum, &n[1], st);
+        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 2)}, ListDst{lb, nullptr}, qp.nrows, qp.bsum, &n[2], st);
+        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 4)}, ListDst{lm, nullptr}, qp.nrows, qp.bsum, &n[4], st);
+        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 3)}, ListDst{lm, &n[4]}, qp.nrows, qp.bsum, &n[3], st);
+        launches += 4 * scan_launches(qp.nrows);
+        BCU(cudaGetLastError());
+        BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));
+        if (op == 0) {
+            const size_t ss_m = (size_t)bm_words * 4 + 16 * kStage * 4;
+            k_b_single_bitmap<<<resident(k_b_single_bitmap, 512, ss_m, sm), 512, ss_m, st>>>(
+                Q, BatchRows{lm, &n[4], &n[3], &qp.next_row[0]}, bm_words);
+            BLAUNCH();
+            const int blk_b = (int)tu.block_threads;
+            const size_t ss_b = ((size_t)1 << tu.block_lg) * 4 + (size_t)(blk_b / 32) * kStage * 4;
+            k_b_single_block<<<resident(k_b_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(
+                Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[1]}, tu.block_lg);
+            BLAUNCH();
+            const uint32_t wps = warps_for(((size_t)(1u << tu.warp_lg) + kStage) * 4);
+            const size_t ss_w = (size_t)wps * ((1u << tu.warp_lg) + kStage) * 4;
+            k_b_single_warp<<<resident(k_b_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(
+                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg);
+            BLAUNCH();
+        } else {
+            const unsigned g_t = (unsigned)(2 * sm);
+            k_b_agg_tile<<<g_t, 512, 0, st>>>(Q, BatchRows{lm, &n[4], &n[3], &qp.next_row[2]}, s->agg_scratch,
+                                              1u << s->tile_lg);
+            BLAUNCH();
+            const size_t ss_b = (size_t)2 << tu.block_lg << 2;
+            k_b_agg_block<<<resident(k_b_agg_block, 256, ss_b, sm), 256, ss_b, st>>>(
+                Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[3]}, tu.block_lg);
+            BLAUNCH();
+            const uint32_t wpa = warps_for((size_t)8 << tu.warp_lg);
+            const size_t ss_w = (size_t)wpa << (tu.warp_lg + 1) << 2;
+            k_b_agg_warp<<<resident(k_b_agg_warp, 32 * wpa, ss_w, sm), 32 * wpa, ss_w, st>>>(
+                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg);
+            BLAUNCH();
+        }
+    }
+    BCU(cudaMemcpyAsync(s->h_res, Q.res, (size_t)nq * sizeof(QueryRes), cudaMemcpyDeviceToHost, st));
+    return DIM3G_OK;
+}
+
+// Shared-memory limits of the batch kernels (per device, idempotent).
+// Limits for the largest settings (tiles of 2^19 bits, 2^14-slot CTA sets,
+// 1024-thread CTAs).
+int set_batch_attributes(dim3g_ctx* ctx) {
+    const int bm = (1 << 19) / 8 + 16 * (int)kStage * 4;
+    const int blk = (1 << 14) * 4 + 32 * (int)kStage * 4;
+    BCU(cudaFuncSetAttribute(k_b_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, bm));
+    BCU(cudaFuncSetAttribute(k_b_single_block, cudaFuncAttributeMaxDynamicSharedMemorySize, blk));
+    BCU(cudaFuncSetAttribute(k_b_single_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    BCU(cudaFuncSetAttribute(k_b_agg_block, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 << 14 << 2));
+    BCU(cudaFuncSetAttribute(k_b_agg_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    return DIM3G_OK;
+}
+
+int ensure_agg_scratch(dim3g_relset* s) {
+    dim3g_ctx* ctx = s->ctx;
+    const size_t need = (size_t)2 * I::sm_count(ctx) * 2 * ((size_t)1 << s->tile_lg) * 4;
+    if (s->agg_bytes >= need) return DIM3G_OK;
+    if (s->agg_scratch) cudaFree(s->agg_scratch);
+    s->agg_scratch = nullptr;
+    s->agg_bytes = 0;
+    if (cudaMalloc(&s->agg_scratch, need) != cudaSuccess) {
+        cudaGetLastError();
+        return I::fail(ctx, DIM3G_ERR_NOMEM, "COUNT scratch: device allocation of %zu bytes failed", need);
+    }
+    // counters start at zero; every row resets the counters it touched
+    BCU(cudaMemset(s->agg_scratch, 0, need));
+    s->agg_bytes = need;
+    return DIM3G_OK;
+}
+
+// Results of a finished pass into the caller's query array.
+int query_results(dim3g_relset* s, const QueryPlan& qp, dim3g_query* q) {
+    int first = DIM3G_OK;
+    for (uint32_t i = 0; i < qp.nq; i++) {
+        const QueryRes& r = s->h_res[i];
+        q[i].swapped = qp.swapped[i];
+        q[i].n_out = r.n_out;
+        q[i].out_j = r.out_j;
+        int st = DIM3G_OK;
+        if (r.err) st = DIM3G_ERR_DEVICE;
+        else if (r.n_out > q[i].capacity) st = DIM3G_ERR_CAPACITY;
+        q[i].status = st;
+        if (st && !first) {
+            first = st;
+            I::fail(s->ctx, st, "query %u: %s", i,
+                    st == DIM3G_ERR_DEVICE ? "device bound violated" : "output buffer too small");
+        }
+    }
+    return first;
+}
+
+int relset_build_sync(dim3g_relset* s, const dim3g_relation* rels) {
+    dim3g_ctx* ctx = s->ctx;
+    cudaStream_t st = I::stream(ctx);
+    for (int attempt = 0; attempt < 2; attempt++) {
+        uint64_t launches = 0;
+        int r = relset_enqueue_build(s, st, launches);
+        I::add_launches(ctx, launches);
+        if (r) return r;
+        BCU(cudaStreamSynchronize(st));
+        const uint64_t need = s->h_need[0];
+        const uint32_t err = (uint32_t)s->h_need[1];
+        if (need <= s->yt_cap) {
+            if (err) return I::fail(ctx, DIM3G_ERR_DEVICE, "relation set build: device bound violated (flags %u)", err);
+            return DIM3G_OK;
+        }
+        r = relset_plan(s, rels, s->nrel, need);  // regrow the (y, tile) pool
+        if (r) return r;
+    }
+    return I::fail(ctx, DIM3G_ERR_DEVICE, "relation set build: key space did not converge");
+}
+
+}  // namespace
+
+// ================================================================== batch
+struct dim3g_batch {
+    dim3g_relset set;
+    QueryPlan qp;
+    std::vector<dim3g_relation> rels;
+    std::vector<dim3g_query> queries;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint64_t launches_per_run = 0;
+    float ms_last = 0;
+    ~dim3g_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+};
+
+namespace {
+
+int batch_capture(dim3g_batch* b) {
+    dim3g_ctx* ctx = b->set.ctx;
+    cudaStream_t st = I::stream(ctx);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    int r = query_upload(&b->set, b->qp);
+    if (r) return r;
+    BCU(cudaStreamSynchronize(st));
+    uint64_t launches = 0;
+    BCU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    r = relset_enqueue_build(&b->set, st, launches);
+    if (!r) r = query_enqueue(&b->set, b->qp, st, launches);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    if (e != cudaSuccess) return I::fail(ctx, DIM3G_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    b->graph = g;
+    BCU(cudaGraphInstantiate(&b->exec, g, 0));
+    b->launches_per_run = launches;
+    return DIM3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dim3g_relset_create(dim3g_ctx* ctx, const dim3g_relation* rels, uint32_t n, dim3g_relset** out) {
+    if (!ctx || !out || (n && !rels)) return DIM3G_ERR_INVALID;
+    *out = nullptr;
+    if (n == 0) return I::fail(ctx, DIM3G_ERR_INVALID, "empty relation set");
+    BCU(cudaSetDevice(I::device(ctx)));
+    dim3g_relset* s = new dim3g_relset();
+    s->ctx = ctx;
+    s->tile_lg = tuning_of(ctx).tile_lg;
+    int r = cudaMallocHost((void**)&s->h_need, 16) == cudaSuccess ? DIM3G_OK
+                                                                   : I::fail(ctx, DIM3G_ERR_NOMEM, "pinned allocation failed");
+    if (!r) r = set_batch_attributes(ctx);
+    if (!r) r = relset_plan(s, rels, n, 0);
+    if (!r) r = relset_build_sync(s, rels);
+    if (r) {
+        delete s;
+        return r;
+    }
+    *out = s;
+    return DIM3G_OK;
+}
+
+void dim3g_relset_destroy(dim3g_relset* s) {
+    if (!s) return;
+    cudaStreamSynchronize(I::stream(s->ctx));
+    delete s;
+}
+
+uint64_t dim3g_relset_bytes(const dim3g_relset* s) { return s ? (uint64_t)(s->mem_bytes + s->qmem_bytes + s->agg_bytes) : 0; }
+
+int dim3g_relset_join(dim3g_relset* s, dim3g_query* q, uint32_t n) {
+    if (!s || (n && !q)) return DIM3G_ERR_INVALID;
+    if (n == 0) return DIM3G_OK;
+    dim3g_ctx* ctx = s->ctx;
+    BCU(cudaSetDevice(I::device(ctx)));
+    cudaStream_t st = I::stream(ctx);
+    QueryPlan qp;
+    int r = query_plan(s, q, n, qp);
+    if (!r && qp.has_count) r = ensure_agg_scratch(s);
+    if (!r) r = query_upload(s, qp);
+    if (r) return r;
+    uint64_t launches = 0;
+    r = query_enqueue(s, qp, st, launches);
+    I::add_launches(ctx, launches);
+    if (r) return r;
+    BCU(cudaStreamSynchronize(st));
+    return query_results(s, qp, q);
+}
+
+int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_query* q, uint32_t n, dim3g_batch** out) {
+    if (!ctx || !out || (n && (!rels || !q))) return DIM3G_ERR_INVALID;
+    *out = nullptr;
+    if (n == 0) return I::fail(ctx, DIM3G_ERR_INVALID, "empty batch");
+    BCU(cudaSetDevice(I::device(ctx)));
+    dim3g_batch* b = new dim3g_batch();
+    b->set.ctx = ctx;
+    b->set.tile_lg = tuning_of(ctx).tile_lg;
+    b->rels.assign(rels, rels + 2 * (size_t)n);
+    b->queries.assign(q, q + n);
+    for (uint32_t i = 0; i < n; i++) {
+        b->queries[i].r = 2 * i;
+        b->queries[i].s = 2 * i + 1;
+    }
+    int r = cudaMallocHost((void**)&b->set.h_need, 16) == cudaSuccess
+                ? DIM3G_OK
+                : I::fail(ctx, DIM3G_ERR_NOMEM, "pinned allocation failed");
+    if (!r && (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess))
+        r = I::fail(ctx, DIM3G_ERR_CUDA, "event creation failed");
+    if (!r) r = set_batch_attributes(ctx);
+    if (!r) r = relset_plan(&b->set, b->rels.data(), 2 * n, 0);
+    if (!r) r = query_plan(&b->set, b->queries.data(), n, b->qp);
+    if (!r && b->qp.has_count) r = ensure_agg_scratch(&b->set);
+    if (!r) r = batch_capture(b);
+    if (r) {
+        delete b;
+        return r;
+    }
+    *out = b;
+    return DIM3G_OK;
+}
+
+int dim3g_batch_run(dim3g_batch* b, dim3g_query* q) {
+    if (!b || !q) return DIM3G_ERR_INVALID;
+    dim3g_ctx* ctx = b->set.ctx;
+    BCU(cudaSetDevice(I::device(ctx)));
+    cudaStream_t st = I::stream(ctx);
+    for (int attempt = 0; attempt < 2; attempt++) {
+        BCU(cudaEventRecord(b->ev0, st));
+        BCU(cudaGraphLaunch(b->exec, st));
+        BCU(cudaEventRecord(b->ev1, st));
+        BCU(cudaStreamSynchronize(st));
+        I::add_launches(ctx, b->launches_per_run);
+        cudaEventElapsedTime(&b->ms_last, b->ev0, b->ev1);
+        const uint64_t need = b->set.h_need[0];
+        if (need <= b->set.yt_cap) {
+            const uint32_t err = (uint32_t)b->set.h_need[1];
+            if (err) return I::fail(ctx, DIM3G_ERR_DEVICE, "batch index build: device bound violated (flags %u)", err);
+            for (uint32_t i = 0; i < b->qp.nq; i++) {
+                q[i].capacity = b->queries[i].capacity;
+                q[i].op = b->queries[i].op;
+            }
+            return query_results(&b->set, b->qp, q);
+        }
+        // the (y, f tile) key space outgrew its pool: re-plan and capture
+        int r = relset_plan(&b->set, b->rels.data(), (uint32_t)b->rels.size(), need);
+        if (!r) r = query_plan(&b->set, b->queries.data(), b->qp.nq, b->qp);
+        if (!r) r = batch_capture(b);
+        if (r) return r;
+    }
+    return I::fail(ctx, DIM3G_ERR_DEVICE, "batch: key space did not converge");
+}
+
+int dim3g_batch_info(const dim3g_batch* b, float* ms_last, uint64_t* launches_per_run, uint64_t* device_bytes) {
+    if (!b) return DIM3G_ERR_INVALID;
+    if (ms_last) *ms_last = b->ms_last;
+    if (launches_per_run) *launches_per_run = b->launches_per_run;
+    if (device_bytes) *device_bytes = (uint64_t)(b->set.mem_bytes + b->set.qmem_bytes + b->set.agg_bytes);
+    return DIM3G_OK;
+}
+
+void dim3g_batch_destroy(dim3g_batch* b) {
+    if (!b) return;
+    cudaStreamSynchronize(I::stream(b->set.ctx));
+    delete b;
+}
+
+}  // extern "C"

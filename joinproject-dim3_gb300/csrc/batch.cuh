@@ -111,6 +111,7 @@ struct RelPools {
     uint32_t* JRf;            // ntot + 1, global positions
     uint32_t* curF;
     uint32_t* ICf;            // global y ids
+    uint32_t* ICr;            // the row (local f id) of each ICf entry
     uint32_t* cnt_yt;         // yt_cap
     uint32_t* JRy;            // yt_cap, global positions
     uint32_t* curY;
@@ -125,7 +126,7 @@ __device__ __forceinline__ DevTable rel_table(unsigned long long* pool, const Re
     return DevTable{pool + r.tab_off, r.tab_cap - 1};
 }
 
-__global__ void k_ix_insert(RelPools P) {
+static __global__ void k_ix_insert(RelPools P) {
     SegCursor sc{P.tup_off, P.nrel};
     DIM3G_FOR_CHUNK(i, P.ntot) {
         const uint32_t r = sc.at(i);
@@ -139,7 +140,7 @@ __global__ void k_ix_insert(RelPools P) {
 }
 
 // One CTA: per-relation id bases, z tiling and (y, tile) key ranges.
-__global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t tile_lg) {
+static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t tile_lg) {
     __shared__ uint64_t sm[1024 / 32 + 1];
     uint64_t cf = 0, cy = 0, ck = 0;
     for (uint32_t b = 0; b < P.nrel; b += 1024) {
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t tile_lg
 }
 
 // Tuples -> (global f id, global y id); degree of f; count of (y, f tile).
-__global__ void k_ix_map(RelPools P) {
+static __global__ void k_ix_map(RelPools P) {
     if (*P.yt_need > P.yt_cap) return;  // layout overflow: the host regrows
     SegCursor sc{P.tup_off, P.nrel};
     DIM3G_FOR_CHUNK(i, P.ntot) {
@@ -195,11 +196,11 @@ __global__ void k_ix_map(RelPools P) {
         P.Pm[i] = make_uint2(fid, yid);
         atomicAdd(&P.degF[fid], 1u);
         const uint64_t key = d.yt_base + (uint64_t)(yid - d.ybase) * d.T + ((fid - d.fbase) >> d.tile_shift);
-        atomicAdd(&P.cnt_yt[key], 1u);
+        atomic_inc_agg(P.cnt_yt, key);  // heavy y keys repeat within a warp
     }
 }
 
-__global__ void k_ix_scatter(RelPools P) {
+static __global__ void k_ix_scatter(RelPools P) {
     if (*P.yt_need > P.yt_cap) return;
     SegCursor sc{P.tup_off, P.nrel};
     DIM3G_FOR_CHUNK(i, P.ntot) {
@@ -208,9 +209,10 @@ __global__ void k_ix_scatter(RelPools P) {
         const uint2 pm = P.Pm[i];
         const uint32_t pos = atomicAdd(&P.curF[pm.x], 1u);
         P.ICf[pos] = pm.y;
+        P.ICr[pos] = pm.x - (uint32_t)d.fbase;
         const uint32_t fl = pm.x - (uint32_t)d.fbase;
         const uint64_t key = d.yt_base + (uint64_t)(pm.y - d.ybase) * d.T + (fl >> d.tile_shift);
-        const uint32_t p2 = atomicAdd(&P.curY[key], 1u);
+        const uint32_t p2 = atomic_inc_agg(P.curY, key);
         P.ICy[p2] = fl;
         P.VSy[p2] = P.in[r].pairs[i - sc.lo].x;
     }
@@ -232,8 +234,8 @@ struct QueryIn {
 struct QueryRes {
     unsigned long long n_out;   // pairs written (or needed when > cap)
     unsigned long long out_j;   // candidates
-    unsigned long long rows[3]; // rows per kernel class: bitmap, block, warp
-    uint32_t err, nx, ny, nz;
+    uint32_t err;
+    uint32_t nx, ny, nz;        // rows (distinct P.f; 0 when a side is empty), P.y, Q.f
 };
 
 struct QueryPools {
@@ -248,6 +250,7 @@ struct QueryPools {
     const uint32_t* id2y;
     const uint32_t* JRf;
     const uint32_t* ICf;
+    const uint32_t* ICr;
     const uint32_t* JRy;
     const uint32_t* ICy;
     const uint32_t* VSy;
@@ -256,13 +259,21 @@ struct QueryPools {
     uint32_t* JRq;    // nrows: P row pointers, relative
     uint32_t* ucap;   // nrows
     uint8_t* cls;     // nrows
+    unsigned long long* wrow;  // nrows: candidates per row
     RowCtx* rc;       // nq
     Reserve* rs;      // nq
     QueryRes* res;    // nq
+    const unsigned long long* yt_need;  // the relation set's key-space check
+    uint64_t yt_cap;
 };
 
+// False when the relation set's (y, f tile) key space outgrew its pool: its
+// CSR was not built, and the query kernels must not read it.
+__device__ __forceinline__ bool layout_ok(const QueryPools& Q) { return *Q.yt_need <= Q.yt_cap; }
+
 // y map: y id of P -> y id of Q, or Q's sentinel y id (no tuples).
-__global__ void k_q_ymap(QueryPools Q) {
+static __global__ void k_q_ymap(QueryPools Q) {
+    if (!layout_ok(Q)) return;
     SegCursor sc{Q.qt_off, Q.nq};
     DIM3G_FOR_CHUNK(i, Q.ntot) {
         const uint32_t qi = sc.at(i);
@@ -278,29 +289,40 @@ __global__ void k_q_ymap(QueryPools Q) {
 }
 
 // P's CSR entries as Q y ids.
-__global__ void k_q_entries(QueryPools Q) {
+static __global__ void k_q_entries(QueryPools Q) {
+    if (!layout_ok(Q)) return;
     SegCursor sc{Q.qt_off, Q.nq};
     DIM3G_FOR_CHUNK(i, Q.ntot) {
         const uint32_t qi = sc.at(i);
         const RelDev& p = Q.rel[Q.qin[qi].p];
-        const uint32_t yg = Q.ICf[p.tup_off + (i - sc.lo)];
-        Q.ICq[i] = Q.ymap[sc.lo + (yg - p.ybase)];
+        const uint64_t e = i - sc.lo;
+        const uint32_t yg = Q.ICf[p.tup_off + e];
+        const uint32_t yq = Q.ymap[sc.lo + (yg - p.ybase)];
+        Q.ICq[i] = yq;
+        // candidates of the entry: its S segment over all z tiles
+        const RelDev& q = Q.rel[Q.qin[qi].q];
+        const uint32_t* jr = Q.JRy + q.yt_base + (uint64_t)yq * q.T;
+        const uint32_t len = jr[q.T] - jr[0];
+        // entries of one row are contiguous: one atomic per run of a row
+        const uint64_t g = Q.qrow_off[qi] + Q.ICr[p.tup_off + e];
+        atomic_add_grouped(&Q.wrow[g], g, len);
     }
 }
 
 // P's row pointers relative to P's first entry.
-__global__ void k_q_rows(QueryPools Q) {
+static __global__ void k_q_rows(QueryPools Q) {
+    if (!layout_ok(Q)) return;
     SegCursor sc{Q.qrow_off, Q.nq};
     DIM3G_FOR_CHUNK(i, Q.nrows) {
         const uint32_t qi = sc.at(i);
         const RelDev& p = Q.rel[Q.qin[qi].p];
         const uint64_t x = i - sc.lo;
-        if (x <= p.nf) Q.JRq[i] = Q.JRf[p.fbase + x] - (uint32_t)p.tup_off;
+        if (x <= Q.res[qi].nx) Q.JRq[i] = Q.JRf[p.fbase + x] - (uint32_t)p.tup_off;
     }
 }
 
 // One thread per query: its row context and output reservation.
-__global__ void k_q_setup(QueryPools Q) {
+static __global__ void k_q_setup(QueryPools Q) {
     const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= Q.nq) return;
     const QueryIn qn = Q.qin[qi];
@@ -326,57 +348,36 @@ __global__ void k_q_setup(QueryPools Q) {
     Q.rc[qi] = c;
     Q.rs[qi] = Reserve{&Q.res[qi].n_out, qn.cap};
     QueryRes r{};
-    r.nx = (uint32_t)p.nf;
+    const bool ok = layout_ok(Q);
+    const bool live = ok && Q.qt_off[qi + 1] > Q.qt_off[qi];  // both sides nonempty
+    r.nx = live ? (uint32_t)p.nf : 0u;
+    r.err = ok ? 0u : (uint32_t)kErrTableFull;
     r.ny = (uint32_t)p.ny;
     r.nz = (uint32_t)q.nf;
     Q.res[qi] = r;
 }
 
-// Per-row work and class (1..4 project, 5..8 COUNT, 0 empty); one warp per
-// row of the row space.
-__global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b) {
-    const uint32_t lane = lane_id();
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint64_t per = (Q.nrows + nwarps - 1) / nwarps;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t g0 = gw * per, g1 = g0 + per < Q.nrows ? g0 + per : Q.nrows;
+// Per-row class (1..4 project, 5..8 COUNT) from the candidates counted per
+// row by k_q_entries; one thread per row of the row space.
+static __global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b) {
+    if (!layout_ok(Q)) return;
     SegCursor sc{Q.qrow_off, Q.nq};
-    unsigned long long acc = 0;
-    uint32_t acc_q = 0xFFFFFFFFu;
-    for (uint64_t g = g0; g < g1; g++) {
+    DIM3G_FOR_CHUNK(g, Q.nrows) {
         const uint32_t qi = sc.at(g);
-        if (qi != acc_q) {
-            if (lane == 0 && acc) atomicAdd(&Q.res[acc_q].out_j, acc);
-            acc = 0;
-            acc_q = qi;
-        }
-        const RowCtx& c = Q.rc[qi];
         const uint64_t x = g - sc.lo;
-        const uint32_t nf = Q.res[qi].nx;
-        if (x >= nf) {
-            if (lane == 0) Q.cls[g] = 0;
-            continue;
+        if (x >= Q.res[qi].nx) continue;
+        const unsigned long long w = Q.wrow[g];
+        const uint32_t m = Q.res[qi].nz;
+        const uint32_t u = (uint32_t)(w < m ? w : m);
+        Q.ucap[g] = u;
+        uint32_t k = row_class(w, u, cap_w, cap_b);
+        if (k && Q.qin[qi].op == kOpCount) {
+            k += 4;
+            if (w >= 0xFFFFFFFFull) raise_error(&Q.res[qi].err, kErrCountRange);
         }
-        const uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
-        unsigned long long w = 0;
-        for (uint32_t e = e0 + lane; e < e1; e += 32) {
-            const uint64_t r = (uint64_t)c.IC_R[e] * c.T;
-            w += c.JR_S[r + c.T] - c.JR_S[r];
-        }
-        w = warp_sum(w);
-        if (lane == 0) {
-            const uint32_t u = (uint32_t)(w < c.m ? w : c.m);
-            Q.ucap[g] = u;
-            uint32_t k = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
-            if (k && Q.qin[qi].op == kOpCount) {
-                k += 4;
-                if (w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
-            }
-            Q.cls[g] = (uint8_t)k;
-            acc += w;
-        }
+        Q.cls[g] = (uint8_t)k;
+        atomic_add_grouped(&Q.res[qi].out_j, qi, w);  // one atomic per query run
     }
-    if (lane == 0 && acc) atomicAdd(&Q.res[acc_q].out_j, acc);
 }
 
 // Row g of the row space -> (query, local row).
@@ -393,14 +394,13 @@ struct BatchRows {
     uint32_t* next;                 // dynamic row counter of CTA classes
 };
 
-// ---- project, single pass (rows of many queries; contexts in shared memory)
-__global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, BatchRows L, uint32_t bitmap_words) {
+// ---- project, single pass: rows of many queries, each CTA (or warp) copying
+// its row's query context into shared memory; the row bodies of single.cuh.
+static __global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, BatchRows L, uint32_t bitmap_words) {
     extern __shared__ uint32_t bm[];
     __shared__ uint32_t s_row, s_x, s_q;
     __shared__ RowCtx s_c;
-    const uint32_t wib = threadIdx.x >> 5;
-    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    uint32_t* stage = bm + bitmap_words + wib * kStage;
+    uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*L.n_a + *L.n_b);
     for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
         if (threadIdx.x == 0) {
@@ -410,31 +410,15 @@ __global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, BatchRow
             s_c = Q.rc[s_q];
         }
         __syncthreads();
-        const RowCtx& c = s_c;
-        const uint32_t x = s_x;
-        StageSink sink{stage, c.out, Q.rs[s_q], c.id2x[x]};
-        for (uint32_t t = 0; t < c.T; t++) {
-            const uint32_t lo = t * c.tile_width;
-            const uint32_t width = min(c.tile_width, c.m - lo);
-            const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
-            uint4* b4 = reinterpret_cast<uint4*>(bm);
-            for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
-            __syncthreads();
-            TileBitmap set{bm, lo};
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
-            __syncthreads();
-        }
-        sink.flush();
+        single_bitmap_row(s_c, Q.rs[s_q], s_x, bm, stage);
     }
 }
 
-__global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
+static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row, s_x, s_q;
     __shared__ RowCtx s_c;
-    const uint32_t wib = threadIdx.x >> 5;
-    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    uint32_t* stage = smem + (1u << block_lg) + wib * kStage;
+    uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
         if (threadIdx.x == 0) {
@@ -444,31 +428,19 @@ __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, BatchRows
             s_c = Q.rc[s_q];
         }
         __syncthreads();
-        const RowCtx& c = s_c;
-        const uint32_t x = s_x;
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
-        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
-        uint4* t4 = reinterpret_cast<uint4*>(smem);
-        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
-            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
-        __syncthreads();
-        HashSet set{smem, lg, c.err};
-        StageSink sink{stage, c.out, Q.rs[s_q], c.id2x[x]};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
-        sink.flush();
+        single_block_row(s_c, Q.rs[s_q], s_x, smem, stage, block_lg);
     }
 }
 
 // Warp class: at most 8 warps per CTA, one context slot each.
-__global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+static __global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ RowCtx s_c[8];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
     uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
-    uint32_t* stage = tab + (1u << warp_lg);
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
-        uint32_t x, qi = 0;
+        uint32_t x = 0, qi = 0;
         if (lane == 0) {
             qi = query_of_row(Q, L.list[ri], &x);
             s_c[wib] = Q.rc[qi];
@@ -476,15 +448,7 @@ __global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L
         qi = __shfl_sync(0xffffffffu, qi, 0);
         x = __shfl_sync(0xffffffffu, x, 0);
         __syncwarp();
-        const RowCtx& c = s_c[wib];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
-        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
-        for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
-        __syncwarp();
-        HashSet set{tab, lg, c.err};
-        StageSink sink{stage, c.out, Q.rs[qi], c.id2x[x]};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
-        sink.flush();
+        single_warp_row(s_c[wib], Q.rs[qi], x, tab, tab + (1u << warp_lg), warp_lg);
         __syncwarp();
     }
 }
@@ -507,7 +471,7 @@ __device__ __forceinline__ void emit_groups(const RowCtx& c, const Reserve& rs, 
     }
 }
 
-__global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ RowCtx s_c[8];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
@@ -515,7 +479,7 @@ __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, u
     uint32_t* vals = keys + (1u << warp_lg);
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
-        uint32_t x, qi = 0;
+        uint32_t x = 0, qi = 0;
         if (lane == 0) {
             qi = query_of_row(Q, L.list[ri], &x);
             s_c[wib] = Q.rc[qi];
@@ -524,7 +488,26 @@ __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, u
         x = __shfl_sync(0xffffffffu, x, 0);
         __syncwarp();
         const RowCtx& c = s_c[wib];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        const Reserve rs = Q.rs[qi];
+        const uint32_t xv = c.id2x[x];
+        unsigned long long* oc = Q.qin[qi].out_cnt;
+        NullSink sink;
+        if (use_row_counters(c.m, u, warp_lg + 1)) {
+            for (uint32_t s = lane; s < c.m; s += 32) keys[s] = 0;
+            __syncwarp();
+            CountTile set{keys, 0};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
+            __syncwarp();
+            for (uint32_t sb = 0; sb < c.m; sb += 32) {
+                const uint32_t z = sb + lane;
+                const uint32_t v = z < c.m ? keys[z] : 0u;
+                emit_groups(c, rs, oc, v != 0, xv, v ? __ldg(&c.id2z[z]) : 0u, v);
+            }
+            __syncwarp();
+            continue;
+        }
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
         for (uint32_t s = lane; s < (1u << lg); s += 32) {
             keys[s] = kEmpty32;
@@ -532,12 +515,8 @@ __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, u
         }
         __syncwarp();
         CountMap set{keys, vals, lg, c.err};
-        NullSink sink;
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
         __syncwarp();
-        const Reserve rs = Q.rs[qi];
-        const uint32_t xv = c.id2x[x];
-        unsigned long long* oc = Q.qin[qi].out_cnt;
         for (uint32_t sb = 0; sb < (1u << lg); sb += 32) {
             const uint32_t key = keys[sb + lane];
             const bool have = key != kEmpty32;
@@ -547,7 +526,7 @@ __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, u
     }
 }
 
-__global__ void __launch_bounds__(256) k_b_agg_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
+static __global__ void __launch_bounds__(256) k_b_agg_block(QueryPools Q, BatchRows L, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row, s_x, s_q;
     __shared__ RowCtx s_c;
@@ -566,24 +545,46 @@ __global__ void __launch_bounds__(256) k_b_agg_block(QueryPools Q, BatchRows L, 
         __syncthreads();
         const RowCtx& c = s_c;
         const uint32_t x = s_x;
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        const bool direct = use_row_counters(c.m, u, block_lg + 1);
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
-        for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
-            keys[s] = kEmpty32;
-            vals[s] = 0;
+        if (direct) {
+            for (uint32_t s = threadIdx.x; s < c.m; s += blockDim.x) keys[s] = 0;
+        } else {
+            for (uint32_t s = threadIdx.x; s < (1u << lg); s += blockDim.x) {
+                keys[s] = kEmpty32;
+                vals[s] = 0;
+            }
         }
         __syncthreads();
-        CountMap set{keys, vals, lg, c.err};
         NullSink sink;
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        if (direct) {
+            CountTile set{keys, 0};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        } else {
+            CountMap set{keys, vals, lg, c.err};
+            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        }
         __syncthreads();
         const Reserve rs = Q.rs[s_q];
         const uint32_t xv = c.id2x[x];
         unsigned long long* oc = Q.qin[s_q].out_cnt;
-        for (uint32_t sb = wib * 32; sb < (1u << lg); sb += nw * 32) {
-            const uint32_t key = keys[sb + lane];
-            const bool have = key != kEmpty32;
-            emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[key]) : 0u, have ? vals[sb + lane] : 0u);
+        const uint32_t span = direct ? c.m : (1u << lg);
+        for (uint32_t sb = wib * 32; sb < span; sb += nw * 32) {
+            const uint32_t s = sb + lane;
+            uint32_t zid = kEmpty32, v = 0;
+            if (s < span) {
+                if (direct) {
+                    v = keys[s];
+                    zid = v ? s : kEmpty32;
+                } else {
+                    zid = keys[s];
+                    v = vals[s];
+                }
+            }
+            const bool have = zid != kEmpty32;
+            emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[zid]) : 0u, have ? v : 0u);
         }
     }
 }
@@ -605,7 +606,7 @@ struct TouchCountTile {
     }
 };
 
-__global__ void __launch_bounds__(512) k_b_agg_tile(QueryPools Q, BatchRows L, uint32_t* scratch, uint32_t tile_cap) {
+static __global__ void __launch_bounds__(512) k_b_agg_tile(QueryPools Q, BatchRows L, uint32_t* scratch, uint32_t tile_cap) {
     __shared__ uint32_t s_row, s_x, s_q, s_nt;
     __shared__ RowCtx s_c;
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();

@@ -52,6 +52,42 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Warp-aggregated increment: every calling lane adds 1 to base[key]; lanes
+// sharing a key get consecutive old values from one atomic (skewed keys
+// would otherwise serialise on one address).  Returns the lane's old value.
+__device__ __forceinline__ uint32_t atomic_inc_agg(uint32_t* base, uint64_t key) {
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, key);
+    const int leader = __ffs(grp) - 1;
+    uint32_t old = 0;
+    if ((int)(threadIdx.x & 31) == leader) old = atomicAdd(&base[key], (uint32_t)__popc(grp));
+    old = __shfl_sync(grp, old, leader);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    return old + __popc(grp & lt);
+}
+
+// Adds v of every calling lane into *dst, lanes grouped by key (the lanes of
+// a group pass the same dst): one atomic per group.  v < 2^48 (larger
+// values are added by the lane alone).  The group sum is formed from three
+// 16-bit slices, each of whose sums fits 32 bits.
+__device__ __forceinline__ void atomic_add_grouped(unsigned long long* dst, uint64_t key, unsigned long long v) {
+    if (v >> 48) {
+        atomicAdd(dst, v);
+        v = 0;
+    }
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, key);
+    const unsigned a = __reduce_add_sync(grp, (unsigned)(v & 0xFFFFu));
+    const unsigned b = __reduce_add_sync(grp, (unsigned)((v >> 16) & 0xFFFFu));
+    const unsigned c = __reduce_add_sync(grp, (unsigned)(v >> 32));
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+        const unsigned long long s =
+            (unsigned long long)a + ((unsigned long long)b << 16) + ((unsigned long long)c << 32);
+        if (s) atomicAdd(dst, s);
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

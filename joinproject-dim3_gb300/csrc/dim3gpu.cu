@@ -22,6 +22,7 @@
 
 #include "../../include/dim3gpu.h"
 #include "aggregate.cuh"
+#include "internal.h"
 #include "common.cuh"
 #include "expand.cuh"
 #include "mapper.cuh"
@@ -151,7 +152,7 @@ template <class Src, class Dst>
 int run_scan(dim3g_ctx* c, Src src, Dst dst, uint64_t n, uint64_t* bsum, unsigned long long* total) {
     device_scan(src, dst, n, bsum, total, c->stream);
     CU(cudaGetLastError());
-    c->launches += n ? 3 : 0;
+    c->launches += scan_launches(n);
     return DIM3G_OK;
 }
 #define SCAN(...)                                \
@@ -254,7 +255,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint2* Pm = ws_get<uint2>(c, jp.nP);
     uint32_t* id2x = ws_get<uint32_t>(c, jp.nP);
     uint32_t* id2z = ws_get<uint32_t>(c, jp.nQ);
-    uint64_t* bsum = ws_get<uint64_t>(c, scan_blocks(capP > capQ ? capP : capQ) + 1);
+    uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(capP > capQ ? capP : capQ));
     if (!sc || !tx.slots || !ty.slots || !tz.slots || !Qk || !Pm || !id2x || !id2z || !bsum)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
 
@@ -315,7 +316,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* lists = ws_get<uint32_t>(c, (uint64_t)3 * n);
     uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
-    uint64_t* bsum2 = ws_get<uint64_t>(c, scan_blocks((nyt > n ? nyt : n) + 1) + 1);
+    uint64_t* bsum2 = ws_get<uint64_t>(c, scan_storage((nyt > n ? nyt : n) + 1));
     if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !VS || !Zq || !ucap || !cls || !lists ||
         !cnt || !off || !bsum2)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
@@ -670,6 +671,22 @@ int host_join(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, u
 
 }  // namespace
 
+namespace dim3g_internal {
+cudaStream_t stream(const dim3g_ctx* c) { return c->stream; }
+int device(const dim3g_ctx* c) { return c->device; }
+int sm_count(const dim3g_ctx* c) { return c->sm_count; }
+void add_launches(dim3g_ctx* c, uint64_t n) { c->launches += n; }
+int fail(dim3g_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+}  // namespace dim3g_internal
+
 // ====================================================================== C ABI
 extern "C" {
 
@@ -937,7 +954,7 @@ int dim3g_mapper_insert(dim3g_mapper* m, const uint32_t* keys, uint64_t n, int32
     uint32_t* dk;
     int32_t* di;
     if ((r = mapper_stage(m, keys, n, &dk, &di))) return r;
-    uint64_t* bsum = ws_get<uint64_t>(c, scan_blocks(n) + 1);
+    uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(n));
     unsigned long long* total = ws_get<unsigned long long>(c, 1);
     uint32_t* err = ws_get<uint32_t>(c, 1);
     if (!bsum || !total || !err) return fail(c, DIM3G_ERR_NOMEM, "mapper scratch allocation failed");

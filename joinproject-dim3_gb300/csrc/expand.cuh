@@ -21,6 +21,32 @@ namespace dim3g {
 
 constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
 constexpr uint32_t kHugeRow = 1u << 16;
+constexpr uint32_t kWarpWorkMax = 1u << 14;  // candidates a single warp takes alone
+
+// A hash-class row dedups with a bitmap over the whole z domain instead of
+// a hash set when that bitmap fits the kernel's table memory (2^slots_lg
+// words) and clearing it costs no more than the row's candidates
+// (m <= 32 u, u = min(candidates, m)): no probing, one atomicOr per
+// candidate.  Small z domains with many duplicate candidates take this path.
+__device__ __forceinline__ bool use_row_bitmap(uint32_t m, uint32_t u, uint32_t slots_lg) {
+    return (uint64_t)m <= (32ull << slots_lg) && (uint64_t)m <= 32ull * u;
+}
+// Row class from its candidates w and u = min(w, m): 1 (one warp) for few
+// distinct z and few candidates, 2 (one CTA, hash set or bitmap) up to
+// cap_b distinct, 3 / 4 (one CTA, z-tile bitmaps; 4 = huge, scheduled
+// first) beyond; 0 for an empty row.
+__device__ __forceinline__ uint32_t row_class(unsigned long long w, uint32_t u, uint32_t cap_w, uint32_t cap_b) {
+    if (u == 0) return 0;
+    if (u <= cap_w && w <= kWarpWorkMax) return 1;
+    if (u <= cap_b) return 2;
+    return u <= kHugeRow ? 3 : 4;
+}
+// Words of a whole-domain bitmap, rounded to uint4 and at least 32 (idle
+// lanes of TileBitmap touch words 0..31).
+__device__ __forceinline__ uint32_t row_bitmap_words(uint32_t m) {
+    const uint32_t w = (((m + 31) >> 5) + 3) & ~3u;
+    return w < 32 ? 32 : w;
+}
 
 struct RowCtx {
     const uint32_t* JR_R;  // n+1 row pointers of R by x id
@@ -238,7 +264,7 @@ __device__ __forceinline__ uint32_t cta_next_row(uint32_t* counter, uint32_t* s_
 
 // Class 1: one warp per row, 2^warp_lg slots per warp.
 template <bool WRITE>
-__global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __restrict__ rows,
                                                    const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
     extern __shared__ uint32_t smem[];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
@@ -246,26 +272,38 @@ __global__ void __launch_bounds__(256) k_rows_warp(RowCtx c, const uint32_t* __r
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        const bool bm = use_row_bitmap(c.m, u, warp_lg);
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
-        for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
+        const uint32_t nclr = bm ? row_bitmap_words(c.m) : (1u << lg);
+        const uint32_t fill = bm ? 0u : kEmpty32;
+        for (uint32_t s = lane; s < nclr; s += 32) tab[s] = fill;
         __syncwarp();
-        HashSet set{tab, lg, c.err};
+        WriteSink wsink{c.out, c.err, 0, 0, 0, nullptr};
+        CountSink csink;
         if (WRITE) {
-            WriteSink sink{c.out, c.err, c.off[x], c.cnt[x], c.id2x[x], nullptr};
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
-        } else {
-            CountSink sink;
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
-            if (lane == 0) c.cnt[x] = sink.count;
+            wsink.base = c.off[x];
+            wsink.lim = c.cnt[x];
+            wsink.xv = c.id2x[x];
         }
+        if (bm) {
+            TileBitmap set{tab, 0};
+            if (WRITE) warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, wsink);
+            else warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, csink);
+        } else {
+            HashSet set{tab, lg, c.err};
+            if (WRITE) warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, wsink);
+            else warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, csink);
+        }
+        if (!WRITE && lane == 0) c.cnt[x] = csink.count;
         __syncwarp();
     }
 }
 
 // Class 2: one CTA per row, 2^block_lg slots.
 template <bool WRITE>
-__global__ void __launch_bounds__(1024) k_rows_block(RowCtx c, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(1024) k_rows_block(RowCtx c, const uint32_t* __restrict__ rows,
                                                     const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_count, s_row;
@@ -274,22 +312,33 @@ __global__ void __launch_bounds__(1024) k_rows_block(RowCtx c, const uint32_t* _
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
+        const uint32_t u = c.ucap[x];
+        const bool bm = use_row_bitmap(c.m, u, block_lg);
+        uint32_t lg = ceil_log2(2 * u);
         lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+        const uint32_t fill = bm ? 0u : kEmpty32;
+        const uint32_t n4 = (bm ? row_bitmap_words(c.m) : (1u << lg)) / 4;
         uint4* t4 = reinterpret_cast<uint4*>(smem);
-        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
-            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
+        for (uint32_t s = threadIdx.x; s < n4; s += blockDim.x) t4[s] = make_uint4(fill, fill, fill, fill);
         if (threadIdx.x == 0) s_count = 0;
         __syncthreads();
-        HashSet set{smem, lg, c.err};
+        WriteSink wsink{c.out, c.err, 0, 0, 0, &s_count};
+        CountSink csink;
         if (WRITE) {
-            WriteSink sink{c.out, c.err, c.off[x], c.cnt[x], c.id2x[x], &s_count};
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
-        } else {
-            CountSink sink;
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
-            if (lane == 0 && sink.count) atomicAdd(&s_count, sink.count);
+            wsink.base = c.off[x];
+            wsink.lim = c.cnt[x];
+            wsink.xv = c.id2x[x];
         }
+        if (bm) {
+            TileBitmap set{smem, 0};
+            if (WRITE) warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, wsink);
+            else warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, csink);
+        } else {
+            HashSet set{smem, lg, c.err};
+            if (WRITE) warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, wsink);
+            else warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, csink);
+        }
+        if (!WRITE && lane == 0 && csink.count) atomicAdd(&s_count, csink.count);
         __syncthreads();
         if (!WRITE && threadIdx.x == 0) c.cnt[x] = s_count;
     }
@@ -298,7 +347,7 @@ __global__ void __launch_bounds__(1024) k_rows_block(RowCtx c, const uint32_t* _
 // Classes 3 and 4: one CTA per row, a bitmap over one z tile at a time.  The
 // row list holds the class-4 rows first; nrows = *n4 + *n3.
 template <bool WRITE>
-__global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uint32_t* __restrict__ rows,
+static __global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uint32_t* __restrict__ rows,
                                                       const unsigned long long* __restrict__ n3,
                                                       const unsigned long long* __restrict__ n4) {
     extern __shared__ uint32_t bm[];
@@ -340,7 +389,7 @@ __global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uint32_t* 
 // the row class (0: empty).  One warp per row.  With check_range set
 // (join-aggregate, 32-bit per-group counters) a row of 2^32 or more
 // candidates raises kErrCountRange.
-__global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range,
+static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range,
                            uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj,
                            unsigned long long* outj_cls) {
     const uint32_t lane = lane_id();
@@ -358,7 +407,7 @@ __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b,
         if (lane == 0) {
             uint32_t u = (uint32_t)(w < c.m ? w : c.m);
             ucap[x] = u;
-            const uint32_t k = u == 0 ? 0 : (u <= cap_w ? 1 : (u <= cap_b ? 2 : (u <= kHugeRow ? 3 : 4)));
+            const uint32_t k = row_class(w, u, cap_w, cap_b);
             cls[x] = (uint8_t)k;
             if (check_range && w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
             acc += w;

@@ -20,7 +20,7 @@ namespace dim3g {
 
 constexpr uint32_t kPendingBit = 0x80000000u;
 
-__global__ void k_mapper_claim(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, uint32_t* err) {
+static __global__ void k_mapper_claim(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, uint32_t* err) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
         const unsigned long long want = ((unsigned long long)key << 32) | (kPendingBit | (uint32_t)i);
@@ -75,14 +75,14 @@ struct AssignNewIdDst {
     }
 };
 
-__global__ void k_mapper_gather(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, int32_t* __restrict__ ids) {
+static __global__ void k_mapper_gather(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, int32_t* __restrict__ ids) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         unsigned long long* s = mapper_slot(t, keys[i]);
         ids[i] = s ? (int32_t)(uint32_t)*s : -1;
     }
 }
 
-__global__ void k_mapper_find(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, int32_t* __restrict__ ids) {
+static __global__ void k_mapper_find(DevTable t, const uint32_t* __restrict__ keys, uint64_t n, int32_t* __restrict__ ids) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t id = table_find(t, keys[i]);
         ids[i] = id == kNotFound ? -1 : (int32_t)id;
@@ -90,7 +90,7 @@ __global__ void k_mapper_find(DevTable t, const uint32_t* __restrict__ keys, uin
 }
 
 // Rehash every settled slot of `from` into `to` (capacity growth).
-__global__ void k_mapper_rehash(DevTable from, DevTable to, uint32_t* err) {
+static __global__ void k_mapper_rehash(DevTable from, DevTable to, uint32_t* err) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= from.mask; i += (uint64_t)gridDim.x * blockDim.x) {
         unsigned long long v = from.slots[i];
         if (v == kEmpty64) continue;

@@ -51,7 +51,7 @@ __device__ __forceinline__ uint32_t table_find(DevTable t, uint32_t key) {
 
 // Build pass over the larger relation P: insert its first column into tx and
 // its y column into ty.
-__global__ void k_insert_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint32_t* err) {
+static __global__ void k_insert_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint32_t* err) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 p = P[i];
         table_insert(tx, p.x, err);
@@ -61,7 +61,7 @@ __global__ void k_insert_p(const uint2* __restrict__ P, uint64_t n, DevTable tx,
 
 // Semi-join of Q against ty (mapping_y's probe, dim3.hpp:816-827): keep the
 // tuples whose y occurs in P as (c, y id), insert their first column into tz.
-__global__ void k_probe_q(const uint2* __restrict__ Q, uint64_t n, DevTable ty, DevTable tz, uint2* __restrict__ Qk,
+static __global__ void k_probe_q(const uint2* __restrict__ Q, uint64_t n, DevTable ty, DevTable tz, uint2* __restrict__ Qk,
                           unsigned long long* nkept, uint32_t* err) {
     for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t i = i0 + threadIdx.x;
@@ -103,7 +103,7 @@ struct AssignIdDst {
 };
 
 // P -> (x id, y id); per-x degree histogram.
-__global__ void k_map_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint2* __restrict__ Pm,
+static __global__ void k_map_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, DevTable ty, uint2* __restrict__ Pm,
                         uint32_t* __restrict__ degx) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 p = P[i];
@@ -116,13 +116,13 @@ __global__ void k_map_p(const uint2* __restrict__ P, uint64_t n, DevTable tx, De
 
 // Q' = (z value, y id) -> z id; histogram over the (y, z tile) CSR key
 // y*T + z/TB.
-__global__ void k_map_q(const uint2* __restrict__ Qk, uint64_t n, DevTable tz, uint32_t T, uint32_t tile_shift,
+static __global__ void k_map_q(const uint2* __restrict__ Qk, uint64_t n, DevTable tz, uint32_t T, uint32_t tile_shift,
                         uint32_t* __restrict__ zid, uint32_t* __restrict__ cnt_yt) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 q = Qk[i];
         uint32_t zi = table_find(tz, q.x);
         zid[i] = zi;
-        atomicAdd(&cnt_yt[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
+        atomic_inc_agg(cnt_yt, (uint64_t)q.y * T + (zi >> tile_shift));  // skewed y repeat within a warp
     }
 }
 
@@ -140,7 +140,7 @@ struct RowPtrDst {
     }
 };
 
-__global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uint32_t* __restrict__ cursor,
+static __global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uint32_t* __restrict__ cursor,
                             uint32_t* __restrict__ ic) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 p = Pm[i];
@@ -151,13 +151,13 @@ __global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uint32_t* 
 
 // S CSR by (y id, z tile): z ids into ic and, beside them, z values into vs
 // (the write pass emits values without a gather through id2z).
-__global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t* __restrict__ zid, uint64_t n, uint32_t T,
+static __global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t* __restrict__ zid, uint64_t n, uint32_t T,
                             uint32_t tile_shift, uint32_t* __restrict__ cursor, uint32_t* __restrict__ ic,
                             uint32_t* __restrict__ vs) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 q = Qk[i];
         uint32_t zi = zid[i];
-        uint32_t pos = atomicAdd(&cursor[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
+        uint32_t pos = atomic_inc_agg(cursor, (uint64_t)q.y * T + (zi >> tile_shift));
         ic[pos] = zi;
         vs[pos] = q.x;
     }

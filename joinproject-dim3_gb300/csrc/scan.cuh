@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_reduce(Src src, uint64_t n,
 
 // Single-block exclusive scan of nb block sums in place; writes the grand
 // total to *total.
-__global__ void __launch_bounds__(1024) k_scan_sums(uint64_t* sums, uint64_t nb, unsigned long long* total) {
+static __global__ void __launch_bounds__(1024) k_scan_sums(uint64_t* sums, uint64_t nb, unsigned long long* total) {
     __shared__ uint64_t sm[1024 / 32 + 1];
     uint64_t carry = 0;
     for (uint64_t c = 0; c < nb; c += 1024) {
@@ -73,9 +73,49 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(Src src, uint64_t n, 
     }
 }
 
-// Host driver.  block_sums must hold scan_blocks(n) entries; total (device)
-// receives the sum of all items.
+// Host driver.  block_sums must hold scan_storage(n) entries; total
+// (device) receives the sum of all items.  Up to kScanSumsDirect block sums
+// are scanned by one CTA; more are scanned by the same three kernels one
+// level up (their own block sums stored after them).
 inline uint64_t scan_blocks(uint64_t n) { return (n + kScanTile - 1) / kScanTile; }
+constexpr uint64_t kScanSumsDirect = 32768;
+inline uint64_t scan_storage(uint64_t n) {
+    uint64_t nb = scan_blocks(n), s = nb + 1;
+    while (nb > kScanSumsDirect) {
+        nb = scan_blocks(nb);
+        s += nb + 1;
+    }
+    return s;
+}
+// Number of kernel launches device_scan makes for n items.
+inline uint64_t scan_launches(uint64_t n) {
+    uint64_t nb = scan_blocks(n), k = 0;
+    if (nb == 0) return 0;
+    k = 3;
+    while (nb > kScanSumsDirect) {
+        nb = scan_blocks(nb);
+        k += 2;
+    }
+    return k;
+}
+
+struct SumsSrc {
+    const uint64_t* a;
+    __device__ uint64_t operator()(uint64_t i) const { return a[i]; }
+};
+// In place: k_scan_apply reads all items of a thread before writing them.
+struct SumsDst {
+    uint64_t* a;
+    __device__ void operator()(uint64_t i, uint64_t e, uint64_t) const { a[i] = e; }
+};
+
+template <class Src, class Dst>
+inline void device_scan(Src src, Dst dst, uint64_t n, uint64_t* block_sums, unsigned long long* total, cudaStream_t st);
+
+inline void scan_block_sums(uint64_t* sums, uint64_t nb, unsigned long long* total, cudaStream_t st) {
+    if (nb <= kScanSumsDirect) k_scan_sums<<<1, 1024, 0, st>>>(sums, nb, total);
+    else device_scan(SumsSrc{sums}, SumsDst{sums}, nb, sums + nb + 1, total, st);
+}
 
 template <class Src, class Dst>
 inline void device_scan(Src src, Dst dst, uint64_t n, uint64_t* block_sums, unsigned long long* total, cudaStream_t st) {
@@ -85,7 +125,7 @@ inline void device_scan(Src src, Dst dst, uint64_t n, uint64_t* block_sums, unsi
         return;
     }
     k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, st>>>(src, n, block_sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(block_sums, nb, total);
+    scan_block_sums(block_sums, nb, total, st);
     k_scan_apply<<<(unsigned)nb, kScanBlock, 0, st>>>(src, n, block_sums, dst);
 }
 

@@ -61,82 +61,123 @@ struct StageSink {
     }
 };
 
-// Class 1, single pass: one warp per row; per warp 2^warp_lg set slots then
-// kStage staging entries.
-__global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
-                                                     const unsigned long long* __restrict__ nrows_p, uint32_t warp_lg) {
-    extern __shared__ uint32_t smem[];
-    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
-    uint32_t* stage = tab + (1u << warp_lg);
-    const uint32_t nrows = (uint32_t)*nrows_p;
-    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
-        const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
-        lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
-        for (uint32_t s = lane; s < (1u << lg); s += 32) tab[s] = kEmpty32;
-        __syncwarp();
-        HashSet set{tab, lg, c.err};
-        StageSink sink{stage, c.out, rs, c.id2x[x]};
+// ---- row bodies (shared by the one-join kernels below and the many-query
+// kernels of batch.cuh)
+
+// Class 1: the calling warp expands row x; its own 2^warp_lg-word table
+// (hash set, or a whole-domain bitmap when use_row_bitmap) and kStage-entry
+// staging buffer.
+__device__ __forceinline__ void single_warp_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* tab,
+                                                uint32_t* stage, uint32_t warp_lg) {
+    const uint32_t lane = lane_id();
+    const uint32_t u = c.ucap[x];
+    const bool bm = use_row_bitmap(c.m, u, warp_lg);
+    uint32_t lg = ceil_log2(2 * u);
+    lg = lg < 5 ? 5 : (lg > warp_lg ? warp_lg : lg);
+    const uint32_t nclr = bm ? row_bitmap_words(c.m) : (1u << lg);
+    const uint32_t fill = bm ? 0u : kEmpty32;
+    for (uint32_t s = lane; s < nclr; s += 32) tab[s] = fill;
+    __syncwarp();
+    StageSink sink{stage, c.out, rs, c.id2x[x]};
+    if (bm) {
+        TileBitmap set{tab, 0};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
-        sink.flush();
+    } else {
+        HashSet set{tab, lg, c.err};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
     }
+    sink.flush();
 }
 
-// Class 2, single pass: one CTA per row; 2^block_lg set slots, then one
-// staging buffer per warp.
-__global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
-                                                      const unsigned long long* __restrict__ nrows_p, uint32_t block_lg) {
-    extern __shared__ uint32_t smem[];
-    __shared__ uint32_t s_row;
+// Class 2: the whole CTA expands row x; a 2^block_lg-word table (hash set or
+// whole-domain bitmap) at smem, one staging buffer per warp.  Called by all
+// threads after a barrier that follows the previous row.
+__device__ __forceinline__ void single_block_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* smem,
+                                                 uint32_t* stage, uint32_t block_lg) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    uint32_t* stage = smem + (1u << block_lg) + wib * kStage;
-    const uint32_t nrows = (uint32_t)*nrows_p;
-    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
-        const uint32_t x = rows[ri];
-        uint32_t lg = ceil_log2(2 * c.ucap[x]);
-        lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
-        uint4* t4 = reinterpret_cast<uint4*>(smem);
-        for (uint32_t s = threadIdx.x; s < (1u << lg) / 4; s += blockDim.x)
-            t4[s] = make_uint4(kEmpty32, kEmpty32, kEmpty32, kEmpty32);
-        __syncthreads();
-        HashSet set{smem, lg, c.err};
-        StageSink sink{stage, c.out, rs, c.id2x[x]};
+    const uint32_t u = c.ucap[x];
+    const bool bm = use_row_bitmap(c.m, u, block_lg);
+    uint32_t lg = ceil_log2(2 * u);
+    lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
+    const uint32_t fill = bm ? 0u : kEmpty32;
+    const uint32_t n4 = (bm ? row_bitmap_words(c.m) : (1u << lg)) / 4;
+    uint4* t4 = reinterpret_cast<uint4*>(smem);
+    for (uint32_t s = threadIdx.x; s < n4; s += blockDim.x) t4[s] = make_uint4(fill, fill, fill, fill);
+    __syncthreads();
+    StageSink sink{stage, c.out, rs, c.id2x[x]};
+    if (bm) {
+        TileBitmap set{smem, 0};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
-        sink.flush();
+    } else {
+        HashSet set{smem, lg, c.err};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
     }
+    sink.flush();
 }
 
-// Classes 3/4, single pass: one CTA per row; a bitmap over one z tile at a
-// time (words rounded up to uint4, at least 32), then one staging buffer per
-// warp.  The staging survives the tiles of a row.
-__global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
-                                                        const unsigned long long* __restrict__ n3,
-                                                        const unsigned long long* __restrict__ n4,
-                                                        uint32_t bitmap_words) {
+// Classes 3/4: the whole CTA expands row x one z tile at a time into a
+// bitmap at bm (words rounded up to uint4, at least 32); the warps' staging
+// survives the tiles of the row.
+__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* bm,
+                                                  uint32_t* stage) {
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    StageSink sink{stage, c.out, rs, c.id2x[x]};
+    for (uint32_t t = 0; t < c.T; t++) {
+        const uint32_t lo = t * c.tile_width;
+        const uint32_t width = min(c.tile_width, c.m - lo);
+        const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
+        uint4* b4 = reinterpret_cast<uint4*>(bm);
+        for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        TileBitmap set{bm, lo};
+        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
+        __syncthreads();
+    }
+    sink.flush();
+}
+
+// ---- one join
+
+// Class 1: one warp per row; per warp 2^warp_lg table words then kStage
+// staging entries.
+static __global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                            const unsigned long long* __restrict__ nrows_p,
+                                                            uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5;
+    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw)
+        single_warp_row(c, rs, rows[ri], tab, tab + (1u << warp_lg), warp_lg);
+}
+
+// Class 2: one CTA per row; 2^block_lg table words, then one staging buffer
+// per warp.
+static __global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                              const unsigned long long* __restrict__ nrows_p,
+                                                              uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_row;
+    uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row))
+        single_block_row(c, rs, rows[ri], smem, stage, block_lg);
+}
+
+// Classes 3/4: one CTA per row; a bitmap of bitmap_words, then one staging
+// buffer per warp.
+static __global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+                                                               const unsigned long long* __restrict__ n3,
+                                                               const unsigned long long* __restrict__ n4,
+                                                               uint32_t bitmap_words) {
     extern __shared__ uint32_t bm[];
     __shared__ uint32_t s_row;
-    const uint32_t wib = threadIdx.x >> 5;
-    const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    uint32_t* stage = bm + bitmap_words + wib * kStage;
+    uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
-    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
-        const uint32_t x = rows[ri];
-        StageSink sink{stage, c.out, rs, c.id2x[x]};
-        for (uint32_t t = 0; t < c.T; t++) {
-            const uint32_t lo = t * c.tile_width;
-            const uint32_t width = min(c.tile_width, c.m - lo);
-            const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
-            uint4* b4 = reinterpret_cast<uint4*>(bm);
-            for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
-            __syncthreads();
-            TileBitmap set{bm, lo};
-            warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
-            __syncthreads();
-        }
-        sink.flush();
-    }
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row))
+        single_bitmap_row(c, rs, rows[ri], bm, stage);
 }
 
 }  // namespace dim3g

@@ -69,7 +69,24 @@ EXPORTS = [
     "dim3g_mapper_create", "dim3g_mapper_destroy", "dim3g_mapper_insert", "dim3g_mapper_find",
     "dim3g_mapper_size", "dim3g_mapper_clear", "dim3g_mapper_set_cnt",
     "dim3g_join_project_noalloc",
+    "dim3g_relset_create", "dim3g_relset_destroy", "dim3g_relset_bytes", "dim3g_relset_join",
+    "dim3g_batch_create", "dim3g_batch_run", "dim3g_batch_info", "dim3g_batch_destroy",
 ]
+
+OP_PROJECT, OP_COUNT = 0, 1
+
+
+class Relation(ctypes.Structure):
+    _fields_ = [("d_pairs", ctypes.c_void_p), ("n", ctypes.c_uint64)]
+
+
+class Query(ctypes.Structure):
+    _fields_ = [
+        ("r", ctypes.c_uint32), ("s", ctypes.c_uint32), ("op", ctypes.c_uint32), ("swapped", ctypes.c_uint32),
+        ("d_out", ctypes.c_void_p), ("d_cnt", ctypes.c_void_p), ("capacity", ctypes.c_uint64),
+        ("n_out", ctypes.c_uint64), ("out_j", ctypes.c_uint64), ("status", ctypes.c_int32),
+        ("pad", ctypes.c_uint32),
+    ]
 
 _lib = None
 
@@ -111,6 +128,18 @@ def load(path=LIB_PATH):
     L.dim3g_mapper_size.restype = ctypes.c_int64
     L.dim3g_mapper_clear.argtypes = [vp]
     L.dim3g_mapper_set_cnt.argtypes = [vp, ctypes.c_int64]
+    relp, qp = ctypes.POINTER(Relation), ctypes.POINTER(Query)
+    L.dim3g_relset_create.argtypes = [vp, relp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.dim3g_relset_destroy.argtypes = [vp]
+    L.dim3g_relset_destroy.restype = None
+    L.dim3g_relset_bytes.argtypes = [vp]
+    L.dim3g_relset_bytes.restype = ctypes.c_uint64
+    L.dim3g_relset_join.argtypes = [vp, qp, ctypes.c_uint32]
+    L.dim3g_batch_create.argtypes = [vp, relp, qp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.dim3g_batch_run.argtypes = [vp, qp]
+    L.dim3g_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_float), _u64p, _u64p]
+    L.dim3g_batch_destroy.argtypes = [vp]
+    L.dim3g_batch_destroy.restype = None
     _lib = L
     return L
 
@@ -237,6 +266,102 @@ class Context:
         return n.value
 
 
+def _queries(specs):
+    """Query array from dicts {r, s, op, out, cnt, capacity}; out / cnt are
+    torch tensors or device addresses."""
+    q = (Query * len(specs))()
+    for i, d in enumerate(specs):
+        q[i].r, q[i].s = d.get("r", 0), d.get("s", 0)
+        q[i].op = d.get("op", OP_PROJECT)
+        q[i].d_out = _ptr(d["out"]).value if d.get("out") is not None else None
+        q[i].d_cnt = _ptr(d["cnt"]).value if d.get("cnt") is not None else None
+        q[i].capacity = d.get("capacity", 0)
+    return q
+
+
+def _results(q):
+    return [{"n_out": x.n_out, "out_j": x.out_j, "status": x.status, "swapped": x.swapped} for x in q]
+
+
+def _relations(rels):
+    """Relation array from (device tensor or address, n) pairs."""
+    arr = (Relation * len(rels))()
+    for i, (t, n) in enumerate(rels):
+        arr[i].d_pairs = _ptr(t).value if n else None
+        arr[i].n = n
+    return arr
+
+
+class RelSet:
+    """Resident relation indexes; joins between them in many-query passes."""
+
+    def __init__(self, ctx, rels):
+        self.ctx, self.L = ctx, ctx.L
+        self.h = ctypes.c_void_p()
+        self._keep = rels
+        arr = _relations(rels)
+        ctx._check(self.L.dim3g_relset_create(ctx.h, arr, len(rels), ctypes.byref(self.h)))
+
+    def bytes(self):
+        return self.L.dim3g_relset_bytes(self.h)
+
+    def join(self, specs, check=True):
+        """Runs the queries in one pass; returns per-query results (and
+        raises on the first failing status when check is set)."""
+        q = _queries(specs)
+        rc = self.L.dim3g_relset_join(self.h, q, len(specs))
+        if check:
+            self.ctx._check(rc)
+        return _results(q)
+
+    def close(self):
+        if self.h:
+            self.L.dim3g_relset_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent joins (R_i, S_i) planned once, each run one CUDA graph."""
+
+    def __init__(self, ctx, pairs, specs):
+        """pairs: [((dR, nR), (dS, nS)), ...]; specs: per-join dicts (op,
+        out, cnt, capacity)."""
+        self.ctx, self.L = ctx, ctx.L
+        self.h = ctypes.c_void_p()
+        self._keep = (pairs, specs)
+        rels = [x for p in pairs for x in p]
+        self.q = _queries(specs)
+        ctx._check(self.L.dim3g_batch_create(ctx.h, _relations(rels), self.q, len(specs), ctypes.byref(self.h)))
+
+    def run(self, check=True):
+        rc = self.L.dim3g_batch_run(self.h, self.q)
+        if check:
+            self.ctx._check(rc)
+        return _results(self.q)
+
+    def info(self):
+        ms, nl, nb = ctypes.c_float(), ctypes.c_uint64(), ctypes.c_uint64()
+        self.ctx._check(self.L.dim3g_batch_info(self.h, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(nb)))
+        return {"ms_last": ms.value, "launches_per_run": nl.value, "device_bytes": nb.value}
+
+    def close(self):
+        if self.h:
+            self.L.dim3g_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Mapper:
     """GPU L+S mapper: value -> dense id with the reference's insert order."""
 
@@ -335,6 +460,47 @@ def batch_params(seed, q, n_lo=1e4, n_hi=4e6, s_lo=0.5, s_hi=1.5, d_lo=1e3, d_hi
 
 
 # Named workloads (the bench and the tests use the same shapes).
+def _zipf_sum_p2(dom, s):
+    k = np.arange(1, dom + 1, dtype=np.float64)
+    w = k ** -s
+    return float((w * w).sum() / w.sum() ** 2)
+
+
+def batch_queries(nq=512, seed=4, n_lo=1e4, n_hi=4e6, s_lo=0.5, s_hi=1.5, d_lo=1e3, d_hi=1e6,
+                  cap_outj=2 ** 28, cap_out=2 ** 26):
+    """Parameters of the mixed batch: per query |R| and |S| log-uniform in
+    [n_lo, n_hi] (drawn separately), B Zipf exponent s uniform in
+    [s_lo, s_hi], dom(A) = dom(C) = dom(B) log-uniform in [d_lo, d_hi].
+    A draw whose expected join size n_R n_S sum(p_b^2) exceeds cap_outj, or
+    whose expected distinct output dom^2 (1 - exp(-E[OUT_J] / dom^2))
+    exceeds cap_out, is redrawn from the next seeded stream (`redraws`
+    counts them), so the whole batch's output fits in device memory."""
+    out = []
+    for i in range(nq):
+        a = 0
+        while True:
+            rng = np.random.default_rng([seed, i, a])
+            nR = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+            nS = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+            s = float(rng.uniform(s_lo, s_hi))
+            dom = int(np.exp(rng.uniform(np.log(d_lo), np.log(d_hi))))
+            ej = nR * nS * _zipf_sum_p2(dom, s)
+            eo = dom * dom * -np.expm1(-ej / (dom * dom))
+            if ej <= cap_outj and eo <= cap_out:
+                break
+            a += 1
+        out.append({"nR": nR, "nS": nS, "s": s, "dom": dom, "redraws": a,
+                    "seed_R": (seed << 40) + 2 * i, "seed_S": (seed << 40) + 2 * i + 1})
+    return out
+
+
+def batch_relations(params):
+    """(R, S) of every query: first column uniform in [0, dom), y Zipf(s)
+    over dom ranks, the same rank -> value map on both sides."""
+    return [(zipf_side(p["nR"], p["dom"], p["dom"], p["s"], p["seed_R"]),
+             zipf_side(p["nS"], p["dom"], p["dom"], p["s"], p["seed_S"])) for p in params]
+
+
 def workload(name, scale=1.0):
     """Seeded synthetic relations by name; scale < 1 shrinks tuple counts."""
     if name == "zipf_1m":  # 1M tuples per side, dom(A)=dom(C)=50k, dom(B)=20k Zipf s=1.0
