@@ -38,6 +38,12 @@ UNIT = "Mpairs/s"
 WORKLOADS = {
     "chung_lu_20m": "self join-project, Chung-Lu 2^21 vertices, beta 2.1, 1e7 samples (~20M directed edges)",
     "zipf_1m": "R,S 1M tuples, dom(A)=dom(C)=50k uniform, dom(B)=20k Zipf s=1.0",
+    "batch512": "512 independent join-projects in one CUDA-graph launch; |R|,|S| log-uniform [1e4, 4e6], "
+                "B Zipf s U[0.5, 1.5], dom(A)=dom(C)=dom(B) log-uniform [1e3, 1e6]; draws with "
+                "E[OUT_J] > 2^28 or E[|OUT|] > 2^26 redrawn",
+    "serve64": "Poisson arrivals (200 req/s) of join-project (75%) / COUNT (25%) requests over 64 resident "
+               "relations, |R| log-uniform [1e6, 1.6e7], B degree exponent U[1.8, 2.5] over 2^18 shared B "
+               "values (per-relation rank order), dom(A) = |R|/4; HBM budget 120 GB",
 }
 
 
@@ -280,6 +286,213 @@ def run_gpu(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def _upload(arrs):
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda() for a in arrs]
+
+
+def run_batch(args, rank, world, local_rank):
+    """512 independent joins as one CUDA-graph launch per step, against the
+    plain drop-in (one dim3g_join_project_device call per query)."""
+    import torch
+    import dim3gpu
+    torch.cuda.set_device(local_rank)
+    params = dim3gpu.batch_queries(nq=args.batch_queries)
+    rels = dim3gpu.batch_relations(params)
+    ctx = dim3gpu.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    dev = _upload([a for rs in rels for a in rs])
+    pairs = [((dev[2 * i], R.shape[0]), (dev[2 * i + 1], S.shape[0])) for i, (R, S) in enumerate(rels)]
+    torch.cuda.synchronize()
+    sizer = dim3gpu.Batch(ctx, pairs, [{"op": 0, "capacity": 0} for _ in rels])
+    need = [r["n_out"] for r in sizer.run(check=False)]
+    sizer.close()
+    outs = [torch.empty((max(n, 1), 2), dtype=torch.int32, device="cuda") for n in need]
+    b = dim3gpu.Batch(ctx, pairs, [{"op": 0, "capacity": n, "out": o} for n, o in zip(need, outs)])
+    for _ in range(args.warmup):
+        b.run()
+    launches0 = ctx.stats()["launches"]
+    dev_ms = []
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            res = b.run()
+            dev_ms.append(b.info()["ms_last"])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+    assert [r["n_out"] for r in res] == need
+    launches = ctx.stats()["launches"] - launches0
+    total = sum(need)
+    outj = sum(r["out_j"] for r in res)
+    # plain drop-in, same inputs, one call per query into one scratch buffer
+    buf = torch.empty((max(max(need), 1), 2), dtype=torch.int32, device="cuda")
+    plain_ms = []
+    for k in range(2):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        got = [ctx.join_project_device(dev[2 * i], R.shape[0], dev[2 * i + 1], S.shape[0], buf, buf.shape[0])
+               for i, (R, S) in enumerate(rels)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+        assert got == need
+    plain = min(plain_ms)
+    peak, peak_kind = load_peaks()
+    ntup = sum(R.shape[0] + S.shape[0] for R, S in rels)
+    alg = 4 * outj + 8 * total + 24 * ntup
+    line = {
+        "metric": METRIC, "value": round(total / (ms / 1e3) / 1e6, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "batch512", "desc": WORKLOADS["batch512"], "queries": len(rels),
+                   "tuples": int(ntup), "n_out": int(total), "out_j": int(outj),
+                   "redraws": int(sum(p["redraws"] for p in params)),
+                   "l2": "inputs and outputs > L2; no flush"},
+        "graph_device_ms": round(sum(dev_ms) / len(dev_ms), 3),
+        "plain_dropin": {"value": round(total / (plain / 1e3) / 1e6, 3), "ms_per_step": round(plain, 3),
+                         "calls": len(rels)},
+        "batch_over_plain": round(plain / ms, 3),
+        "roofline": {"bound": "hbm", "kernel": "whole graph (index build + query pass)",
+                     "achieved": round(alg / (ms / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4), "traffic": None,
+                     "alg_bytes_per_launch": int(alg)},
+        "gpu_launches": launches, "launches_per_step": b.info()["launches_per_run"],
+        "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
+    ctx.close()
+
+
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
+
+
+def run_serve(args, rank, world, local_rank):
+    """Poisson request stream over a resident set: served (continuous
+    batching) and, on the same trace, the plain drop-in one call at a time."""
+    import queue
+    import torch
+    import dim3gpu
+    torch.cuda.set_device(local_rank)
+    params = dim3gpu.serve_params(scale=args.serve_scale)
+    rels = [dim3gpu.serve_relation(p) for p in params]
+    n = len(rels)
+    dev = _upload(rels)
+    ctx = dim3gpu.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    rs = dim3gpu.RelSet(ctx, [(d, a.shape[0]) for d, a in zip(dev, rels)])
+    build_s = time.perf_counter() - t
+    srv = dim3gpu.Server(rs, lanes=args.lanes, max_batch=64, budget_bytes=args.budget_gb << 30)
+    rng = np.random.default_rng(11)
+    nreq = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, nreq))
+    # a uniformly chosen pair of two different relations (a skewed
+    # relation joined with itself has OUT_J ~ |R|^2 sum p^2, ~1e13)
+    rr = rng.integers(0, n, nreq)
+    ss = (rr + 1 + rng.integers(0, n - 1, nreq)) % n
+    ops = (rng.random(nreq) < 0.25).astype(int)
+    for k in range(min(8, nreq)):  # warm-up requests (not in the trace)
+        tk = srv.submit(int(rr[k]), int(ss[k]), int(ops[k]))
+        srv.wait(tk)
+        srv.release(tk)
+    tickets = queue.Queue()
+    done = []
+
+    def waiter():
+        while True:
+            tk = tickets.get()
+            if tk is None:
+                return
+            res = srv.wait(tk)
+            done.append(res)
+            srv.release(tk)
+
+    th = threading.Thread(target=waiter, daemon=True)
+    th.start()
+    launches0 = ctx.stats()["launches"]
+    refused = []
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        try:
+            for i in range(nreq):
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                try:
+                    tickets.put(srv.submit(int(rr[i]), int(ss[i]), int(ops[i])))
+                except dim3gpu.Dim3GError:
+                    refused.append(i)  # reservation above the whole output budget
+        finally:
+            tickets.put(None)
+        th.join(timeout=args.duration * 10 + 60)
+        wall = time.perf_counter() - t0
+    if th.is_alive():
+        raise RuntimeError("served requests did not complete")
+    launches = ctx.stats()["launches"] - launches0
+    st = srv.stats()
+    lat = [(r["t_done"] - r["t_submit"]) * 1e3 for r in done]
+    pairs = sum(r["n_out"] for r in done)
+    span = max(r["t_done"] for r in done) - min(r["t_submit"] for r in done)
+    bad = sum(1 for r in done if r["status"] != 0)
+    srv.close()
+    # the plain drop-in on the same trace: one call at a time, in arrival order
+    cap = int(max(r["n_out"] for r in done))  # the served results are exact
+    out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device="cuda")
+    cnt = torch.empty((max(cap, 1),), dtype=torch.int64, device="cuda")
+    plain_lat, plain_pairs = [], 0
+    t0 = time.perf_counter()
+    nplain = 0
+    refused_set = set(refused)
+    for i in range(nreq):
+        if i in refused_set:
+            continue
+        now = time.perf_counter() - t0
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        a, b_ = int(rr[i]), int(ss[i])
+        if ops[i]:
+            k = ctx.join_count_device(dev[a], rels[a].shape[0], dev[b_], rels[b_].shape[0], out, cnt, cap)
+        else:
+            k = ctx.join_project_device(dev[a], rels[a].shape[0], dev[b_], rels[b_].shape[0], out, cap)
+        plain_pairs += k
+        plain_lat.append((time.perf_counter() - t0 - arrivals[i]) * 1e3)
+        nplain += 1
+        if time.perf_counter() - t0 > args.duration * 3:
+            break
+    plain_span = time.perf_counter() - t0
+    line = {
+        "metric": METRIC, "value": round(pairs / span / 1e6, 3), "unit": UNIT, "n_gpus": world,
+        "steps": nreq, "warmup": 8, "ms_per_step": round(span / max(len(done), 1) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "serve64", "desc": WORKLOADS["serve64"], "relations": n,
+                   "tuples": int(sum(a.shape[0] for a in rels)), "rate_per_s": args.rate,
+                   "duration_s": args.duration, "lanes": args.lanes, "budget_gb": args.budget_gb,
+                   "l2": "relations and outputs > L2; no flush"},
+        "latency_ms": {"p50": round(_pct(lat, 50), 3), "p99": round(_pct(lat, 99), 3),
+                       "max": round(max(lat), 3)},
+        "requests": len(done), "failed": bad, "refused": len(refused), "passes": st["passes"],
+        "wall_s": round(wall, 3),
+        "relset_build_s": round(build_s, 3),
+        "plain_dropin": {"value": round(plain_pairs / plain_span / 1e6, 3), "requests": nplain,
+                         "latency_ms": {"p50": round(_pct(plain_lat, 50), 3), "p99": round(_pct(plain_lat, 99), 3)}},
+        "gpu_launches": launches, "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    rs.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,12 +504,22 @@ def main():
     ap.add_argument("--cpu-parts", type=int, default=64)
     ap.add_argument("--traffic", type=float, default=None)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-queries", type=int, default=512)
+    ap.add_argument("--serve-scale", type=float, default=1.0)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--lanes", type=int, default=2)
+    ap.add_argument("--budget-gb", type=int, default=120)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batch512":
+        run_batch(args, rank, world, local_rank)
+    elif args.workload == "serve64":
+        run_serve(args, rank, world, local_rank)
     else:
         run_gpu(args, rank, world, local_rank)
 

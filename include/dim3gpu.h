@@ -178,6 +178,53 @@ uint64_t dim3g_relset_bytes(const dim3g_relset* set);
  * when all are DIM3G_OK, else the first failing status. */
 int dim3g_relset_join(dim3g_relset* set, dim3g_query* q, uint32_t n);
 
+/* Exact join size OUT_J of every ordered pair of the set's relations:
+ * outj[r * n + s] = sum over y of deg_R(y) * deg_S(y) (R = relation r,
+ * S = relation s; n = relations in the set).  One GPU pass; synchronous. */
+int dim3g_relset_pair_outj(dim3g_relset* set, uint64_t* outj);
+
+/* ---- serving: continuous batching over a resident relation set ---------
+ * A server runs requests (a relation pair of the set and an op) on `lanes`
+ * CUDA streams, each lane with its own query scratch.  Requests queue on
+ * submit.  A lane that is free admits queued requests in arrival order
+ * while their output reservations fit the budget, runs them as one query
+ * pass and completes them; while one lane's pass runs on the GPU another
+ * lane admits and launches the requests that arrived meanwhile, so passes
+ * overlap on the device.  A request's reservation is
+ * min(OUT_J, distinct R.first x distinct S.first) pairs (8 bytes each, plus
+ * 8 for a COUNT), OUT_J exact from the set's pair matrix, so no request can
+ * overflow its output.  Outputs are device memory held by the server until
+ * the request is released.  budget_bytes bounds the device memory of the
+ * whole serving system: the set, the lanes' scratch and every admitted
+ * request's output.  Results are the same as from dim3g_relset_join. */
+typedef struct dim3g_server dim3g_server;
+typedef struct {
+    uint64_t ticket;
+    int32_t status;         /* DIM3G_OK or the request's error status */
+    uint32_t swapped;       /* 1 when the pairs are (z, x) */
+    uint64_t n_out, out_j;
+    const uint32_t* d_out;  /* device pairs, valid until released */
+    const uint64_t* d_cnt;  /* device counts (DIM3G_OP_COUNT) */
+    double t_submit, t_start, t_done; /* seconds since the server started */
+    uint32_t pass_size;     /* requests in the pass that ran it */
+    uint32_t lane;
+} dim3g_result;
+int dim3g_server_create(dim3g_relset* set, uint32_t lanes, uint32_t max_batch, uint64_t budget_bytes,
+                        dim3g_server** srv);
+/* Queues a request; DIM3G_ERR_NOMEM if its reservation exceeds the output
+ * budget (it could never be admitted). */
+int dim3g_server_submit(dim3g_server* srv, uint32_t r, uint32_t s, uint32_t op, uint64_t* ticket);
+/* Blocks until the request has completed and fills *out. */
+int dim3g_server_wait(dim3g_server* srv, uint64_t ticket, dim3g_result* out);
+/* Frees the request's output and returns its reservation to the budget. */
+int dim3g_server_release(dim3g_server* srv, uint64_t ticket);
+/* Completed requests, query passes run, output bytes reserved now, and the
+ * output budget (budget_bytes less the set and the lanes' scratch). */
+int dim3g_server_stats(const dim3g_server* srv, uint64_t* completed, uint64_t* passes, uint64_t* reserved_bytes,
+                       uint64_t* output_budget);
+/* Finishes queued requests, then stops the lanes and frees all outputs. */
+void dim3g_server_destroy(dim3g_server* srv);
+
 /* ---- batches of independent joins, one CUDA graph --------------------
  * n joins, each with its own device R (rels[2i]) and S (rels[2i+1]),
  * planned once: the index build of all 2n relations and the query pass are

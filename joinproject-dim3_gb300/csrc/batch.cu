@@ -1,5 +1,6 @@
 // batch.cu -- resident relation sets, many-query passes, and batches of
-// independent joins run as one CUDA graph (host side; kernels in batch.cuh).
+// independent joins run as one CUDA graph, and a serving loop with
+// continuous batching over a resident set (host side; kernels in batch.cuh).
 //
 // Relation set build (one stream, no host synchronisation inside):
 //   memsets -> k_ix_insert -> k_ix_layout -> id scans (TF, TY) -> k_ix_map
@@ -19,6 +20,15 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/dim3gpu.h"
@@ -97,6 +107,25 @@ uint32_t warps_for(size_t per_warp) {
 }  // namespace
 
 // ============================================================ relation set
+// Device scratch of one query pass (a relation set has one; every lane of a
+// server has its own, so passes can run concurrently).
+struct QueryScratch {
+    char* qmem = nullptr;
+    size_t qmem_bytes = 0;
+    uint32_t* agg = nullptr;  // COUNT tile counters + touched lists
+    size_t agg_bytes = 0;
+    QueryRes* h_res = nullptr;  // pinned
+    uint32_t h_res_n = 0;
+    QueryScratch() = default;
+    QueryScratch(const QueryScratch&) = delete;
+    QueryScratch& operator=(const QueryScratch&) = delete;
+    ~QueryScratch() {
+        if (qmem) cudaFree(qmem);
+        if (agg) cudaFree(agg);
+        if (h_res) cudaFreeHost(h_res);
+    }
+};
+
 struct dim3g_relset {
     dim3g_ctx* ctx = nullptr;
     uint32_t nrel = 0;
@@ -109,21 +138,12 @@ struct dim3g_relset {
     RelPools P{};
     uint64_t* bsum = nullptr;
     uint64_t bsum_n = 0;
-    // query pass scratch (grow-only)
-    char* qmem = nullptr;
-    size_t qmem_bytes = 0;
-    uint32_t* agg_scratch = nullptr;
-    size_t agg_bytes = 0;
-    QueryRes* h_res = nullptr;  // pinned
-    uint32_t h_res_n = 0;
+    QueryScratch qs;  // scratch of dim3g_relset_join (grow-only)
     unsigned long long* h_need = nullptr;  // pinned: yt keys needed, err
     uint64_t launches_build = 0;
 
     ~dim3g_relset() {
         if (mem) cudaFree(mem);
-        if (qmem) cudaFree(qmem);
-        if (agg_scratch) cudaFree(agg_scratch);
-        if (h_res) cudaFreeHost(h_res);
         if (h_need) cudaFreeHost(h_need);
     }
 };
@@ -163,7 +183,7 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
                  o_ICf = L.add<uint32_t>(s->ntot), o_ICr = L.add<uint32_t>(s->ntot), o_cyt = L.add<uint32_t>(s->yt_cap),
                  o_JRy = L.add<uint32_t>(s->yt_cap), o_curY = L.add<uint32_t>(s->yt_cap),
                  o_ICy = L.add<uint32_t>(s->ntot), o_VSy = L.add<uint32_t>(s->ntot), o_err = L.add<uint32_t>(4),
-                 o_need = L.add<unsigned long long>(2);
+                 o_need = L.add<unsigned long long>(2), o_yoff = L.add<uint64_t>(n + 1);
     uint64_t sn = scan_storage(s->tabtot);
     const uint64_t s2 = scan_storage(s->ntot + 1), s3 = scan_storage(s->yt_cap);
     if (s2 > sn) sn = s2;
@@ -209,6 +229,7 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
     P.VSy = (uint32_t*)(m + o_VSy);
     P.err = (uint32_t*)(m + o_err);
     P.yt_need = (unsigned long long*)(m + o_need);
+    P.yoff = (uint64_t*)(m + o_yoff);
     s->bsum = (uint64_t*)(m + o_bsum);
     s->bsum_n = sn;
     BCU(cudaMemcpy((void*)P.in, s->h_in.data(), n * sizeof(RelIn), cudaMemcpyHostToDevice));
@@ -273,7 +294,35 @@ struct QueryPlan {
     uint64_t* bsum = nullptr;
 };
 
-int query_plan(dim3g_relset* s, const dim3g_query* q, uint32_t nq, QueryPlan& qp) {
+// Device layout of a query pass's scratch (every size monotone in the
+// arguments, so scratch laid out for maxima fits every smaller pass).
+struct QLayout {
+    size_t qin, qt, qr, ymap, ICq, JRq, ucap, cls, wrow, rc, rs, res, lists, ncls, next, bsum, total;
+};
+QLayout query_layout(uint32_t nq, uint64_t ntot, uint64_t nrows) {
+    Layout L;
+    QLayout o;
+    o.qin = L.add<QueryIn>(nq);
+    o.qt = L.add<uint64_t>(nq + 1);
+    o.qr = L.add<uint64_t>(nq + 1);
+    o.ymap = L.add<uint32_t>(ntot);
+    o.ICq = L.add<uint32_t>(ntot);
+    o.JRq = L.add<uint32_t>(nrows);
+    o.ucap = L.add<uint32_t>(nrows);
+    o.cls = L.add<uint8_t>(nrows);
+    o.wrow = L.add<unsigned long long>(nrows);
+    o.rc = L.add<RowCtx>(nq);
+    o.rs = L.add<Reserve>(nq);
+    o.res = L.add<QueryRes>(nq);
+    o.lists = L.add<uint32_t>(4 * nrows);
+    o.ncls = L.add<unsigned long long>(16);
+    o.next = L.add<uint32_t>(8);
+    o.bsum = L.add<uint64_t>(scan_storage(nrows));
+    o.total = L.total;
+    return o;
+}
+
+int query_plan(dim3g_relset* s, QueryScratch& qs, const dim3g_query* q, uint32_t nq, QueryPlan& qp) {
     dim3g_ctx* ctx = s->ctx;
     qp.nq = nq;
     qp.h_qin.resize(nq);
@@ -312,44 +361,37 @@ int query_plan(dim3g_relset* s, const dim3g_query* q, uint32_t nq, QueryPlan& qp
     if (qp.nrows >= 0xFFFFFFFFull)
         return I::fail(ctx, DIM3G_ERR_UNSUPPORTED, "a query pass covers fewer than 2^32-1 rows in total");
 
-    Layout L;
-    const size_t o_qin = L.add<QueryIn>(nq), o_qt = L.add<uint64_t>(nq + 1), o_qr = L.add<uint64_t>(nq + 1),
-                 o_ymap = L.add<uint32_t>(qp.ntot), o_ICq = L.add<uint32_t>(qp.ntot), o_JRq = L.add<uint32_t>(qp.nrows),
-                 o_ucap = L.add<uint32_t>(qp.nrows), o_cls = L.add<uint8_t>(qp.nrows),
-                 o_wrow = L.add<unsigned long long>(qp.nrows), o_rc = L.add<RowCtx>(nq),
-                 o_rs = L.add<Reserve>(nq), o_res = L.add<QueryRes>(nq), o_lists = L.add<uint32_t>(3 * qp.nrows),
-                 o_ncls = L.add<unsigned long long>(16), o_next = L.add<uint32_t>(8),
-                 o_bsum = L.add<uint64_t>(scan_storage(qp.nrows));
-    if (s->qmem && s->qmem_bytes < L.total) {
-        cudaFree(s->qmem);
-        s->qmem = nullptr;
-        s->qmem_bytes = 0;
+    const QLayout o = query_layout(nq, qp.ntot, qp.nrows);
+    if (qs.qmem && qs.qmem_bytes < o.total) {
+        cudaFree(qs.qmem);
+        qs.qmem = nullptr;
+        qs.qmem_bytes = 0;
     }
-    if (!s->qmem) {
-        if (cudaMalloc(&s->qmem, L.total) != cudaSuccess) {
+    if (!qs.qmem) {
+        if (cudaMalloc(&qs.qmem, o.total) != cudaSuccess) {
             cudaGetLastError();
-            return I::fail(ctx, DIM3G_ERR_NOMEM, "query pass: device allocation of %zu bytes failed", L.total);
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "query pass: device allocation of %zu bytes failed", o.total);
         }
-        s->qmem_bytes = L.total;
+        qs.qmem_bytes = o.total;
     }
-    if (s->h_res_n < nq) {
-        if (s->h_res) cudaFreeHost(s->h_res);
-        s->h_res = nullptr;
-        s->h_res_n = 0;
-        if (cudaMallocHost((void**)&s->h_res, (size_t)nq * sizeof(QueryRes)) != cudaSuccess) {
+    if (qs.h_res_n < nq) {
+        if (qs.h_res) cudaFreeHost(qs.h_res);
+        qs.h_res = nullptr;
+        qs.h_res_n = 0;
+        if (cudaMallocHost((void**)&qs.h_res, (size_t)nq * sizeof(QueryRes)) != cudaSuccess) {
             cudaGetLastError();
             return I::fail(ctx, DIM3G_ERR_NOMEM, "query pass: pinned allocation failed");
         }
-        s->h_res_n = nq;
+        qs.h_res_n = nq;
     }
-    char* m = s->qmem;
+    char* m = qs.qmem;
     QueryPools& Q = qp.Q;
     const RelPools& P = s->P;
     Q.rel = P.rel;
-    Q.qin = (const QueryIn*)(m + o_qin);
+    Q.qin = (const QueryIn*)(m + o.qin);
     Q.nq = nq;
-    Q.qt_off = (const uint64_t*)(m + o_qt);
-    Q.qrow_off = (const uint64_t*)(m + o_qr);
+    Q.qt_off = (const uint64_t*)(m + o.qt);
+    Q.qrow_off = (const uint64_t*)(m + o.qr);
     Q.ntot = qp.ntot;
     Q.nrows = qp.nrows;
     Q.TY = P.TY;
@@ -363,19 +405,19 @@ int query_plan(dim3g_relset* s, const dim3g_query* q, uint32_t nq, QueryPlan& qp
     Q.VSy = P.VSy;
     Q.yt_need = P.yt_need;
     Q.yt_cap = P.yt_cap;
-    Q.ymap = (uint32_t*)(m + o_ymap);
-    Q.ICq = (uint32_t*)(m + o_ICq);
-    Q.JRq = (uint32_t*)(m + o_JRq);
-    Q.ucap = (uint32_t*)(m + o_ucap);
-    Q.cls = (uint8_t*)(m + o_cls);
-    Q.wrow = (unsigned long long*)(m + o_wrow);
-    Q.rc = (RowCtx*)(m + o_rc);
-    Q.rs = (Reserve*)(m + o_rs);
-    Q.res = (QueryRes*)(m + o_res);
-    qp.lists = (uint32_t*)(m + o_lists);
-    qp.ncls = (unsigned long long*)(m + o_ncls);
-    qp.next_row = (uint32_t*)(m + o_next);
-    qp.bsum = (uint64_t*)(m + o_bsum);
+    Q.ymap = (uint32_t*)(m + o.ymap);
+    Q.ICq = (uint32_t*)(m + o.ICq);
+    Q.JRq = (uint32_t*)(m + o.JRq);
+    Q.ucap = (uint32_t*)(m + o.ucap);
+    Q.cls = (uint8_t*)(m + o.cls);
+    Q.wrow = (unsigned long long*)(m + o.wrow);
+    Q.rc = (RowCtx*)(m + o.rc);
+    Q.rs = (Reserve*)(m + o.rs);
+    Q.res = (QueryRes*)(m + o.res);
+    qp.lists = (uint32_t*)(m + o.lists);
+    qp.ncls = (unsigned long long*)(m + o.ncls);
+    qp.next_row = (uint32_t*)(m + o.next);
+    qp.bsum = (uint64_t*)(m + o.bsum);
     return DIM3G_OK;
 }
 
@@ -394,7 +436,7 @@ struct ClassList {
 };
 
 // The query pass (stream ordered; capturable).
-int query_enqueue(dim3g_relset* s, QueryPlan& qp, cudaStream_t st, uint64_t& launches) {
+int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t st, uint64_t& launches) {
     dim3g_ctx* ctx = s->ctx;
     QueryPools& Q = qp.Q;
     const int sm = I::sm_count(ctx);
@@ -420,17 +462,19 @@ int query_enqueue(dim3g_relset* s, QueryPlan& qp, cudaStream_t st, uint64_t& lau
     uint32_t* lw = qp.lists;
     uint32_t* lb = qp.lists + qp.nrows;
     uint32_t* lm = qp.lists + 2 * qp.nrows;
+    uint32_t* lt = qp.lists + 3 * qp.nrows;
     const uint32_t bm_words = (1u << s->tile_lg) / 32;  // the tiling the set was built with
     for (int op = 0; op < 2; op++) {
         if (op == 0 && !qp.has_project) continue;
         if (op == 1 && !qp.has_count) continue;
-        const uint8_t k0 = op ? 4 : 0;
-        unsigned long long* n = qp.ncls + 4 * op;  // n[1..4]: rows of classes k0+1..k0+4
+        const uint8_t k0 = op ? 8 : 0;
+        unsigned long long* n = qp.ncls + 8 * op;  // n[1..5]: rows of classes k0+1..k0+5
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 1)}, ListDst{lw, nullptr}, qp.nrows, qp.bsum, &n[1], st);
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 2)}, ListDst{lb, nullptr}, qp.nrows, qp.bsum, &n[2], st);
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 4)}, ListDst{lm, nullptr}, qp.nrows, qp.bsum, &n[4], st);
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 3)}, ListDst{lm, &n[4]}, qp.nrows, qp.bsum, &n[3], st);
-        launches += 4 * scan_launches(qp.nrows);
+        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 5)}, ListDst{lt, nullptr}, qp.nrows, qp.bsum, &n[5], st);
+        launches += 5 * scan_launches(qp.nrows);
         BCU(cudaGetLastError());
         BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));
         if (op == 0) {
@@ -443,28 +487,38 @@ int query_enqueue(dim3g_relset* s, QueryPlan& qp, cudaStream_t st, uint64_t& lau
             k_b_single_block<<<resident(k_b_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(
                 Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[1]}, tu.block_lg);
             BLAUNCH();
-            const uint32_t wps = warps_for(((size_t)(1u << tu.warp_lg) + kStage) * 4);
-            const size_t ss_w = (size_t)wps * ((1u << tu.warp_lg) + kStage) * 4;
+            const uint32_t wps = warps_for(warp_row_words(tu.warp_lg, kStage) * 4);
+            const size_t ss_w = (size_t)wps * warp_row_words(tu.warp_lg, kStage) * 4;
             k_b_single_warp<<<resident(k_b_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(
-                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg);
+                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg, kStage);
+            BLAUNCH();
+            const uint32_t wpt = warps_for(warp_row_words(kTinyLg, kTinyStage) * 4);
+            const size_t ss_t = (size_t)wpt * warp_row_words(kTinyLg, kTinyStage) * 4;
+            k_b_single_warp<<<resident(k_b_single_warp, 32 * wpt, ss_t, sm), 32 * wpt, ss_t, st>>>(
+                Q, BatchRows{lt, &n[5], nullptr, nullptr}, kTinyLg, kTinyStage);
             BLAUNCH();
         } else {
             const unsigned g_t = (unsigned)(2 * sm);
-            k_b_agg_tile<<<g_t, 512, 0, st>>>(Q, BatchRows{lm, &n[4], &n[3], &qp.next_row[2]}, s->agg_scratch,
+            k_b_agg_tile<<<g_t, 512, 0, st>>>(Q, BatchRows{lm, &n[4], &n[3], &qp.next_row[2]}, qs.agg,
                                               1u << s->tile_lg);
             BLAUNCH();
             const size_t ss_b = (size_t)2 << tu.block_lg << 2;
             k_b_agg_block<<<resident(k_b_agg_block, 256, ss_b, sm), 256, ss_b, st>>>(
                 Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[3]}, tu.block_lg);
             BLAUNCH();
-            const uint32_t wpa = warps_for((size_t)8 << tu.warp_lg);
-            const size_t ss_w = (size_t)wpa << (tu.warp_lg + 1) << 2;
+            const uint32_t wpa = warps_for(agg_warp_words(tu.warp_lg, kStage) * 4);
+            const size_t ss_w = (size_t)wpa * agg_warp_words(tu.warp_lg, kStage) * 4;
             k_b_agg_warp<<<resident(k_b_agg_warp, 32 * wpa, ss_w, sm), 32 * wpa, ss_w, st>>>(
-                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg);
+                Q, BatchRows{lw, &n[1], nullptr, nullptr}, tu.warp_lg, kStage);
+            BLAUNCH();
+            const uint32_t wpt = warps_for(agg_warp_words(kTinyLg, kTinyStage) * 4);
+            const size_t ss_t = (size_t)wpt * agg_warp_words(kTinyLg, kTinyStage) * 4;
+            k_b_agg_warp<<<resident(k_b_agg_warp, 32 * wpt, ss_t, sm), 32 * wpt, ss_t, st>>>(
+                Q, BatchRows{lt, &n[5], nullptr, nullptr}, kTinyLg, kTinyStage);
             BLAUNCH();
         }
     }
-    BCU(cudaMemcpyAsync(s->h_res, Q.res, (size_t)nq * sizeof(QueryRes), cudaMemcpyDeviceToHost, st));
+    BCU(cudaMemcpyAsync(qs.h_res, Q.res, (size_t)nq * sizeof(QueryRes), cudaMemcpyDeviceToHost, st));
     return DIM3G_OK;
 }
 
@@ -482,28 +536,28 @@ int set_batch_attributes(dim3g_ctx* ctx) {
     return DIM3G_OK;
 }
 
-int ensure_agg_scratch(dim3g_relset* s) {
+int ensure_agg_scratch(dim3g_relset* s, QueryScratch& qs) {
     dim3g_ctx* ctx = s->ctx;
     const size_t need = (size_t)2 * I::sm_count(ctx) * 2 * ((size_t)1 << s->tile_lg) * 4;
-    if (s->agg_bytes >= need) return DIM3G_OK;
-    if (s->agg_scratch) cudaFree(s->agg_scratch);
-    s->agg_scratch = nullptr;
-    s->agg_bytes = 0;
-    if (cudaMalloc(&s->agg_scratch, need) != cudaSuccess) {
+    if (qs.agg_bytes >= need) return DIM3G_OK;
+    if (qs.agg) cudaFree(qs.agg);
+    qs.agg = nullptr;
+    qs.agg_bytes = 0;
+    if (cudaMalloc(&qs.agg, need) != cudaSuccess) {
         cudaGetLastError();
         return I::fail(ctx, DIM3G_ERR_NOMEM, "COUNT scratch: device allocation of %zu bytes failed", need);
     }
     // counters start at zero; every row resets the counters it touched
-    BCU(cudaMemset(s->agg_scratch, 0, need));
-    s->agg_bytes = need;
+    BCU(cudaMemset(qs.agg, 0, need));
+    qs.agg_bytes = need;
     return DIM3G_OK;
 }
 
 // Results of a finished pass into the caller's query array.
-int query_results(dim3g_relset* s, const QueryPlan& qp, dim3g_query* q) {
+int query_results(dim3g_relset* s, const QueryScratch& qs, const QueryPlan& qp, dim3g_query* q) {
     int first = DIM3G_OK;
     for (uint32_t i = 0; i < qp.nq; i++) {
-        const QueryRes& r = s->h_res[i];
+        const QueryRes& r = qs.h_res[i];
         q[i].swapped = qp.swapped[i];
         q[i].n_out = r.n_out;
         q[i].out_j = r.out_j;
@@ -577,7 +631,7 @@ int batch_capture(dim3g_batch* b) {
     uint64_t launches = 0;
     BCU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     r = relset_enqueue_build(&b->set, st, launches);
-    if (!r) r = query_enqueue(&b->set, b->qp, st, launches);
+    if (!r) r = query_enqueue(&b->set, b->set.qs, b->qp, st, launches);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (r) {
@@ -622,7 +676,9 @@ void dim3g_relset_destroy(dim3g_relset* s) {
     delete s;
 }
 
-uint64_t dim3g_relset_bytes(const dim3g_relset* s) { return s ? (uint64_t)(s->mem_bytes + s->qmem_bytes + s->agg_bytes) : 0; }
+uint64_t dim3g_relset_bytes(const dim3g_relset* s) {
+    return s ? (uint64_t)(s->mem_bytes + s->qs.qmem_bytes + s->qs.agg_bytes) : 0;
+}
 
 int dim3g_relset_join(dim3g_relset* s, dim3g_query* q, uint32_t n) {
     if (!s || (n && !q)) return DIM3G_ERR_INVALID;
@@ -631,16 +687,16 @@ int dim3g_relset_join(dim3g_relset* s, dim3g_query* q, uint32_t n) {
     BCU(cudaSetDevice(I::device(ctx)));
     cudaStream_t st = I::stream(ctx);
     QueryPlan qp;
-    int r = query_plan(s, q, n, qp);
-    if (!r && qp.has_count) r = ensure_agg_scratch(s);
+    int r = query_plan(s, s->qs, q, n, qp);
+    if (!r && qp.has_count) r = ensure_agg_scratch(s, s->qs);
     if (!r) r = query_upload(s, qp);
     if (r) return r;
     uint64_t launches = 0;
-    r = query_enqueue(s, qp, st, launches);
+    r = query_enqueue(s, s->qs, qp, st, launches);
     I::add_launches(ctx, launches);
     if (r) return r;
     BCU(cudaStreamSynchronize(st));
-    return query_results(s, qp, q);
+    return query_results(s, s->qs, qp, q);
 }
 
 int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_query* q, uint32_t n, dim3g_batch** out) {
@@ -664,8 +720,8 @@ int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_q
         r = I::fail(ctx, DIM3G_ERR_CUDA, "event creation failed");
     if (!r) r = set_batch_attributes(ctx);
     if (!r) r = relset_plan(&b->set, b->rels.data(), 2 * n, 0);
-    if (!r) r = query_plan(&b->set, b->queries.data(), n, b->qp);
-    if (!r && b->qp.has_count) r = ensure_agg_scratch(&b->set);
+    if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), n, b->qp);
+    if (!r && b->qp.has_count) r = ensure_agg_scratch(&b->set, b->set.qs);
     if (!r) r = batch_capture(b);
     if (r) {
         delete b;
@@ -695,11 +751,11 @@ int dim3g_batch_run(dim3g_batch* b, dim3g_query* q) {
                 q[i].capacity = b->queries[i].capacity;
                 q[i].op = b->queries[i].op;
             }
-            return query_results(&b->set, b->qp, q);
+            return query_results(&b->set, b->set.qs, b->qp, q);
         }
         // the (y, f tile) key space outgrew its pool: re-plan and capture
         int r = relset_plan(&b->set, b->rels.data(), (uint32_t)b->rels.size(), need);
-        if (!r) r = query_plan(&b->set, b->queries.data(), b->qp.nq, b->qp);
+        if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), b->qp.nq, b->qp);
         if (!r) r = batch_capture(b);
         if (r) return r;
     }
@@ -710,7 +766,7 @@ int dim3g_batch_info(const dim3g_batch* b, float* ms_last, uint64_t* launches_pe
     if (!b) return DIM3G_ERR_INVALID;
     if (ms_last) *ms_last = b->ms_last;
     if (launches_per_run) *launches_per_run = b->launches_per_run;
-    if (device_bytes) *device_bytes = (uint64_t)(b->set.mem_bytes + b->set.qmem_bytes + b->set.agg_bytes);
+    if (device_bytes) *device_bytes = (uint64_t)(b->set.mem_bytes + b->set.qs.qmem_bytes + b->set.qs.agg_bytes);
     return DIM3G_OK;
 }
 
@@ -718,6 +774,361 @@ void dim3g_batch_destroy(dim3g_batch* b) {
     if (!b) return;
     cudaStreamSynchronize(I::stream(b->set.ctx));
     delete b;
+}
+
+}  // extern "C"
+
+// ================================================================ serving
+namespace {
+
+struct SrvReq {
+    uint32_t r = 0, s = 0, op = 0;
+    uint64_t cap = 0;    // reserved pairs
+    uint64_t bytes = 0;  // reserved output bytes
+    uint64_t rows = 0;   // entries of the driving relation (lane scratch)
+    void* d_out = nullptr;
+    void* d_cnt = nullptr;
+    double t_submit = 0, t_start = 0, t_done = 0;
+    int32_t status = 0;
+    uint32_t swapped = 0, pass_size = 0, lane = 0;
+    uint64_t n_out = 0, out_j = 0;
+    bool done = false;
+};
+
+struct Lane {
+    cudaStream_t st = nullptr;
+    QueryScratch qs;
+    QueryPlan qp;
+    QueryIn* h_qin = nullptr;  // pinned staging of the pass's descriptors
+    uint64_t* h_qt = nullptr;
+    uint64_t* h_qr = nullptr;
+    std::thread th;
+    ~Lane() {
+        if (h_qin) cudaFreeHost(h_qin);
+        if (h_qt) cudaFreeHost(h_qt);
+        if (h_qr) cudaFreeHost(h_qr);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+}  // namespace
+
+struct dim3g_server {
+    dim3g_relset* set = nullptr;
+    dim3g_ctx* ctx = nullptr;
+    uint32_t max_batch = 0;
+    uint64_t entries_cap = 0;  // entries of driving relations one pass may hold
+    uint64_t out_budget = 0, reserved = 0;
+    std::vector<uint64_t> outj, nt;  // pair matrix; tuples per relation
+    std::vector<uint64_t> nf;        // distinct first values per relation
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<SrvReq*> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<SrvReq>> reqs;
+    uint64_t next_ticket = 1, completed = 0, passes = 0;
+    bool stop = false;
+    std::vector<std::unique_ptr<Lane>> lanes;
+    cudaStream_t free_st = nullptr;
+    cudaMemPool_t pool = nullptr;
+    std::chrono::steady_clock::time_point t0;
+
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+
+// One lane: admit, run one pass, complete; until stopped with nothing queued.
+void lane_main(dim3g_server* S, uint32_t li) {
+    Lane& L = *S->lanes[li];
+    dim3g_relset* set = S->set;
+    cudaSetDevice(I::device(S->ctx));
+    std::vector<SrvReq*> batch;
+    std::vector<dim3g_query> qv;
+    for (;;) {
+        batch.clear();
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv_work.wait(lk, [&] {
+                return (S->stop && S->pending.empty()) ||
+                       (!S->pending.empty() && S->reserved + S->pending.front()->bytes <= S->out_budget);
+            });
+            if (S->pending.empty()) return;  // stopping
+            uint64_t entries = 0;
+            while (!S->pending.empty() && batch.size() < S->max_batch) {
+                SrvReq* q = S->pending.front();
+                if (S->reserved + q->bytes > S->out_budget) break;
+                if (!batch.empty() && entries + q->rows > S->entries_cap) break;
+                S->reserved += q->bytes;
+                entries += q->rows;
+                batch.push_back(q);
+                S->pending.pop_front();
+            }
+        }
+        const double ts = S->now();
+        const uint32_t n = (uint32_t)batch.size();
+        qv.assign(n, dim3g_query{});
+        int rc = DIM3G_OK;
+        for (uint32_t i = 0; i < n && !rc; i++) {
+            SrvReq* q = batch[i];
+            const size_t pb = (size_t)(q->cap ? q->cap : 1) * 8;
+            if (cudaMallocFromPoolAsync(&q->d_out, pb, S->pool, L.st) != cudaSuccess ||
+                (q->op == DIM3G_OP_COUNT && cudaMallocFromPoolAsync(&q->d_cnt, pb, S->pool, L.st) != cudaSuccess)) {
+                cudaGetLastError();
+                rc = DIM3G_ERR_NOMEM;
+            }
+            qv[i].r = q->r;
+            qv[i].s = q->s;
+            qv[i].op = q->op;
+            qv[i].d_out = (uint32_t*)q->d_out;
+            qv[i].d_cnt = (uint64_t*)q->d_cnt;
+            qv[i].capacity = q->cap;
+        }
+        uint64_t launches = 0;
+        if (!rc) rc = query_plan(set, L.qs, qv.data(), n, L.qp);
+        if (!rc) {
+            const QueryPlan& qp = L.qp;
+            memcpy(L.h_qin, qp.h_qin.data(), n * sizeof(QueryIn));
+            memcpy(L.h_qt, qp.h_qt_off.data(), (n + 1) * 8);
+            memcpy(L.h_qr, qp.h_qrow_off.data(), (n + 1) * 8);
+            if (cudaMemcpyAsync((void*)qp.Q.qin, L.h_qin, n * sizeof(QueryIn), cudaMemcpyHostToDevice, L.st) ||
+                cudaMemcpyAsync((void*)qp.Q.qt_off, L.h_qt, (n + 1) * 8, cudaMemcpyHostToDevice, L.st) ||
+                cudaMemcpyAsync((void*)qp.Q.qrow_off, L.h_qr, (n + 1) * 8, cudaMemcpyHostToDevice, L.st))
+                rc = DIM3G_ERR_CUDA;
+        }
+        if (!rc) rc = query_enqueue(set, L.qs, L.qp, L.st, launches);
+        if (!rc && cudaStreamSynchronize(L.st) != cudaSuccess) rc = DIM3G_ERR_CUDA;
+        const double td = S->now();
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (uint32_t i = 0; i < n; i++) {
+                SrvReq* q = batch[i];
+                if (rc) {
+                    q->status = rc;
+                } else {
+                    const QueryRes& r = L.qs.h_res[i];
+                    q->n_out = r.n_out;
+                    q->out_j = r.out_j;
+                    q->swapped = L.qp.swapped[i];
+                    q->status = r.err ? DIM3G_ERR_DEVICE : (r.n_out > q->cap ? DIM3G_ERR_CAPACITY : DIM3G_OK);
+                }
+                q->t_start = ts;
+                q->t_done = td;
+                q->pass_size = n;
+                q->lane = li;
+                q->done = true;
+            }
+            S->completed += n;
+            S->passes++;
+            I::add_launches(S->ctx, launches);
+        }
+        S->cv_done.notify_all();
+        S->cv_work.notify_all();
+    }
+}
+
+int pair_outj(dim3g_relset* s, uint64_t* outj) {
+    dim3g_ctx* ctx = s->ctx;
+    cudaStream_t st = I::stream(ctx);
+    const size_t nb = (size_t)s->nrel * s->nrel * 8;
+    unsigned long long* d = nullptr;
+    BCU(cudaMalloc(&d, nb));
+    cudaError_t e = cudaMemsetAsync(d, 0, nb, st);
+    if (e == cudaSuccess) {
+        k_pair_outj<<<elem_grid(s->ntot, I::sm_count(ctx)), 256, 0, st>>>(s->P, d);
+        e = cudaGetLastError();
+        I::add_launches(ctx, 1);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(outj, d, nb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) return I::fail(ctx, DIM3G_ERR_CUDA, "pair matrix: %s", cudaGetErrorString(e));
+    return DIM3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dim3g_relset_pair_outj(dim3g_relset* s, uint64_t* outj) {
+    if (!s || !outj) return DIM3G_ERR_INVALID;
+    dim3g_ctx* ctx = s->ctx;
+    BCU(cudaSetDevice(I::device(ctx)));
+    return pair_outj(s, outj);
+}
+
+int dim3g_server_create(dim3g_relset* set, uint32_t lanes, uint32_t max_batch, uint64_t budget_bytes,
+                        dim3g_server** out) {
+    if (!set || !out || lanes == 0 || lanes > 16 || max_batch == 0) return DIM3G_ERR_INVALID;
+    *out = nullptr;
+    dim3g_ctx* ctx = set->ctx;
+    BCU(cudaSetDevice(I::device(ctx)));
+    std::unique_ptr<dim3g_server> S(new dim3g_server());
+    S->set = set;
+    S->ctx = ctx;
+    S->max_batch = max_batch;
+    S->t0 = std::chrono::steady_clock::now();
+    const uint32_t n = set->nrel;
+    S->outj.assign((size_t)n * n, 0);
+    int r = pair_outj(set, S->outj.data());
+    if (r) return r;
+    // distinct first values per relation (the layout the build computed)
+    std::vector<RelDev> rel(n);
+    BCU(cudaMemcpy(rel.data(), set->P.rel, n * sizeof(RelDev), cudaMemcpyDeviceToHost));
+    S->nf.resize(n);
+    S->nt.resize(n);
+    uint64_t max_nt = 1;
+    for (uint32_t i = 0; i < n; i++) {
+        S->nf[i] = rel[i].nf;
+        S->nt[i] = rel[i].nt;
+        if (rel[i].nt > max_nt) max_nt = rel[i].nt;
+    }
+    S->entries_cap = 4 * max_nt > ((uint64_t)1 << 25) ? 4 * max_nt : ((uint64_t)1 << 25);
+    // lanes: stream, scratch sized for the largest pass, pinned staging
+    uint64_t fixed = dim3g_relset_bytes(set);
+    for (uint32_t li = 0; li < lanes; li++) {
+        std::unique_ptr<Lane> L(new Lane());
+        BCU(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking));
+        const QLayout o = query_layout(max_batch, S->entries_cap, S->entries_cap + max_batch);
+        if (cudaMalloc(&L->qs.qmem, o.total) != cudaSuccess) {
+            cudaGetLastError();
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "server lane scratch of %zu bytes", o.total);
+        }
+        L->qs.qmem_bytes = o.total;
+        if (cudaMallocHost((void**)&L->qs.h_res, (size_t)max_batch * sizeof(QueryRes)) != cudaSuccess ||
+            cudaMallocHost((void**)&L->h_qin, (size_t)max_batch * sizeof(QueryIn)) != cudaSuccess ||
+            cudaMallocHost((void**)&L->h_qt, (size_t)(max_batch + 1) * 8) != cudaSuccess ||
+            cudaMallocHost((void**)&L->h_qr, (size_t)(max_batch + 1) * 8) != cudaSuccess) {
+            cudaGetLastError();
+            return I::fail(ctx, DIM3G_ERR_NOMEM, "server lane pinned staging");
+        }
+        L->qs.h_res_n = max_batch;
+        r = ensure_agg_scratch(set, L->qs);
+        if (r) return r;
+        fixed += L->qs.qmem_bytes + L->qs.agg_bytes;
+        S->lanes.push_back(std::move(L));
+    }
+    if (fixed >= budget_bytes)
+        return I::fail(ctx, DIM3G_ERR_NOMEM, "budget %llu bytes below the set and lane scratch (%llu bytes)",
+                       (unsigned long long)budget_bytes, (unsigned long long)fixed);
+    S->out_budget = budget_bytes - fixed;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = I::device(ctx);
+    BCU(cudaMemPoolCreate(&S->pool, &props));
+    uint64_t keep = ~0ull;
+    BCU(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    BCU(cudaStreamCreateWithFlags(&S->free_st, cudaStreamNonBlocking));
+    dim3g_server* raw = S.release();
+    for (uint32_t li = 0; li < lanes; li++) raw->lanes[li]->th = std::thread(lane_main, raw, li);
+    *out = raw;
+    return DIM3G_OK;
+}
+
+int dim3g_server_submit(dim3g_server* S, uint32_t r, uint32_t s, uint32_t op, uint64_t* ticket) {
+    if (!S || !ticket) return DIM3G_ERR_INVALID;
+    const uint32_t n = S->set->nrel;
+    if (r >= n || s >= n || (op != DIM3G_OP_PROJECT && op != DIM3G_OP_COUNT)) return DIM3G_ERR_INVALID;
+    std::unique_ptr<SrvReq> q(new SrvReq());
+    q->r = r;
+    q->s = s;
+    q->op = op;
+    const uint64_t oj = S->outj[(size_t)r * n + s];
+    const double grid = (double)S->nf[r] * (double)S->nf[s];
+    q->cap = (double)oj < grid ? oj : (uint64_t)grid;
+    q->bytes = align256((size_t)(q->cap ? q->cap : 1) * 8) * (op == DIM3G_OP_COUNT ? 2 : 1);
+    q->rows = S->nt[r] > S->nt[s] ? S->nt[r] : S->nt[s];
+    if (q->bytes > S->out_budget || q->rows > S->entries_cap) return DIM3G_ERR_NOMEM;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->stop) return DIM3G_ERR_INVALID;
+        q->t_submit = S->now();
+        *ticket = S->next_ticket++;
+        S->pending.push_back(q.get());
+        S->reqs[*ticket] = std::move(q);
+    }
+    S->cv_work.notify_all();
+    return DIM3G_OK;
+}
+
+int dim3g_server_wait(dim3g_server* S, uint64_t ticket, dim3g_result* out) {
+    if (!S || !out) return DIM3G_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return DIM3G_ERR_INVALID;
+    SrvReq* q = it->second.get();
+    S->cv_done.wait(lk, [&] { return q->done; });
+    out->ticket = ticket;
+    out->status = q->status;
+    out->swapped = q->swapped;
+    out->n_out = q->n_out;
+    out->out_j = q->out_j;
+    out->d_out = (const uint32_t*)q->d_out;
+    out->d_cnt = (const uint64_t*)q->d_cnt;
+    out->t_submit = q->t_submit;
+    out->t_start = q->t_start;
+    out->t_done = q->t_done;
+    out->pass_size = q->pass_size;
+    out->lane = q->lane;
+    return DIM3G_OK;
+}
+
+int dim3g_server_release(dim3g_server* S, uint64_t ticket) {
+    if (!S) return DIM3G_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto it = S->reqs.find(ticket);
+        if (it == S->reqs.end() || !it->second->done) return DIM3G_ERR_INVALID;
+        SrvReq* q = it->second.get();
+        if (q->d_out) cudaFreeAsync(q->d_out, S->free_st);
+        if (q->d_cnt) cudaFreeAsync(q->d_cnt, S->free_st);
+        S->reserved -= q->bytes;
+        S->reqs.erase(it);
+    }
+    S->cv_work.notify_all();
+    return DIM3G_OK;
+}
+
+int dim3g_server_stats(const dim3g_server* S, uint64_t* completed, uint64_t* passes, uint64_t* reserved_bytes,
+                       uint64_t* output_budget) {
+    if (!S) return DIM3G_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(const_cast<dim3g_server*>(S)->mu);
+    if (completed) *completed = S->completed;
+    if (passes) *passes = S->passes;
+    if (reserved_bytes) *reserved_bytes = S->reserved;
+    if (output_budget) *output_budget = S->out_budget;
+    return DIM3G_OK;
+}
+
+void dim3g_server_destroy(dim3g_server* S) {
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+        // completed, unreleased outputs go back to the budget so queued
+        // requests can still be admitted and finished
+        for (auto& kv : S->reqs) {
+            SrvReq* q = kv.second.get();
+            if (!q->done) continue;
+            if (q->d_out) cudaFreeAsync(q->d_out, S->free_st);
+            if (q->d_cnt) cudaFreeAsync(q->d_cnt, S->free_st);
+            q->d_out = q->d_cnt = nullptr;
+            S->reserved -= q->bytes;
+            q->bytes = 0;
+        }
+    }
+    S->cv_work.notify_all();
+    for (auto& L : S->lanes)
+        if (L->th.joinable()) L->th.join();
+    for (auto& kv : S->reqs) {
+        SrvReq* q = kv.second.get();
+        if (q->d_out) cudaFreeAsync(q->d_out, S->free_st);
+        if (q->d_cnt) cudaFreeAsync(q->d_cnt, S->free_st);
+    }
+    cudaStreamSynchronize(S->free_st);
+    cudaStreamDestroy(S->free_st);
+    if (S->pool) cudaMemPoolDestroy(S->pool);
+    delete S;
 }
 
 }  // extern "C"

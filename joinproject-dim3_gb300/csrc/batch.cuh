@@ -120,6 +120,7 @@ struct RelPools {
     uint32_t* VSy;            // f values
     uint32_t* err;            // device error flags of the set
     unsigned long long* yt_need;  // keys the layout needs (+1)
+    uint64_t* yoff;           // nrel + 1: first global y id of each relation
 };
 
 __device__ __forceinline__ DevTable rel_table(unsigned long long* pool, const RelDev& r) {
@@ -172,12 +173,14 @@ static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t 
             d.tile_width = T > 1 ? (1u << tile_lg) : (uint32_t)(nf > 0 ? nf : 1);
             d.pad = 0;
             P.rel[r] = d;
+            P.yoff[r] = d.ybase;
         }
         cf += tf;
         cy += ty;
         ck += tk;
     }
     if (threadIdx.x == 0) {
+        P.yoff[P.nrel] = cy;
         *P.yt_need = ck + 1;
         if (ck + 1 > P.yt_cap) raise_error(P.err, kErrTableFull);
     }
@@ -215,6 +218,30 @@ static __global__ void k_ix_scatter(RelPools P) {
         const uint32_t p2 = atomic_inc_agg(P.curY, key);
         P.ICy[p2] = fl;
         P.VSy[p2] = P.in[r].pairs[i - sc.lo].x;
+    }
+}
+
+// Exact join size of every ordered relation pair (r, s):
+// outj[r * nrel + s] = sum over y of deg_r(y) * deg_s(y).  One thread per y
+// of the set (global y ids), probing every relation's y table.
+static __global__ void k_pair_outj(RelPools P, unsigned long long* outj) {
+    if (*P.yt_need > P.yt_cap) return;
+    const uint64_t ny_all = P.yoff[P.nrel];
+    SegCursor sc{P.yoff, P.nrel};
+    DIM3G_FOR_CHUNK(g, ny_all) {
+        const uint32_t r = sc.at(g);
+        const RelDev& d = P.rel[r];
+        const uint32_t* jr = P.JRy + d.yt_base + (g - sc.lo) * d.T;
+        const unsigned long long deg_r = jr[d.T] - jr[0];
+        const uint32_t v = P.id2y[g];
+        for (uint32_t s = 0; s < P.nrel; s++) {
+            const RelDev& e = P.rel[s];
+            const uint32_t t = table_find(rel_table(P.TY, e), v);
+            if (t == kNotFound) continue;
+            const uint32_t* js = P.JRy + e.yt_base + (uint64_t)(t - e.ybase) * e.T;
+            const uint64_t key = (uint64_t)r * P.nrel + s;
+            atomic_add_grouped(&outj[key], key, deg_r * (js[e.T] - js[0]));
+        }
     }
 }
 
@@ -357,7 +384,7 @@ static __global__ void k_q_setup(QueryPools Q) {
     Q.res[qi] = r;
 }
 
-// Per-row class (1..4 project, 5..8 COUNT) from the candidates counted per
+// Per-row class (1..5 project, 9..13 COUNT) from the candidates counted per
 // row by k_q_entries; one thread per row of the row space.
 static __global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b) {
     if (!layout_ok(Q)) return;
@@ -370,9 +397,9 @@ static __global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b
         const uint32_t m = Q.res[qi].nz;
         const uint32_t u = (uint32_t)(w < m ? w : m);
         Q.ucap[g] = u;
-        uint32_t k = row_class(w, u, cap_w, cap_b);
+        uint32_t k = row_class(w, u, cap_w, cap_b, true);
         if (k && Q.qin[qi].op == kOpCount) {
-            k += 4;
+            k += 8;
             if (w >= 0xFFFFFFFFull) raise_error(&Q.res[qi].err, kErrCountRange);
         }
         Q.cls[g] = (uint8_t)k;
@@ -433,24 +460,34 @@ static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, Ba
 }
 
 // Warp class: at most 8 warps per CTA, one context slot each.
-static __global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+static __global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, BatchRows L, uint32_t warp_lg,
+                                                              uint32_t stage) {
     extern __shared__ uint32_t smem[];
     __shared__ RowCtx s_c[8];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
+    uint32_t* tab = smem + (size_t)wib * warp_row_words(warp_lg, stage);
+    // the warp's pairs are staged across its rows and flushed when the
+    // query (cursor and output) changes
+    PairStageSink sink{reinterpret_cast<uint2*>(tab + (1u << warp_lg)), nullptr, Reserve{nullptr, 0}, 0, stage};
+    uint32_t cur_q = 0xFFFFFFFFu;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         uint32_t x = 0, qi = 0;
-        if (lane == 0) {
-            qi = query_of_row(Q, L.list[ri], &x);
-            s_c[wib] = Q.rc[qi];
-        }
+        if (lane == 0) qi = query_of_row(Q, L.list[ri], &x);
         qi = __shfl_sync(0xffffffffu, qi, 0);
         x = __shfl_sync(0xffffffffu, x, 0);
-        __syncwarp();
-        single_warp_row(s_c[wib], Q.rs[qi], x, tab, tab + (1u << warp_lg), warp_lg);
-        __syncwarp();
+        if (qi != cur_q) {
+            sink.flush();
+            __syncwarp();
+            if (lane == 0) s_c[wib] = Q.rc[qi];
+            __syncwarp();
+            sink.rs = Q.rs[qi];
+            sink.out = s_c[wib].out;
+            cur_q = qi;
+        }
+        single_warp_row(s_c[wib], x, tab, sink, warp_lg);
     }
+    sink.flush();
 }
 
 // ---- COUNT, single pass: rows reserve output ranges from their query's
@@ -471,27 +508,80 @@ __device__ __forceinline__ void emit_groups(const RowCtx& c, const Reserve& rs, 
     }
 }
 
-static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, uint32_t warp_lg) {
+// (x, z, count) groups staged across the rows of one warp and one query,
+// reserved once per kStage groups (see PairStageSink).
+struct GroupStage {
+    uint2* pairs;      // cap (x value, z value)
+    uint32_t* counts;  // cap counts
+    uint2* out;
+    unsigned long long* out_cnt;
+    Reserve rs;
+    uint32_t cap;      // at least 32
+    uint32_t n = 0;
+    __device__ __forceinline__ void flush() {
+        if (n == 0) return;
+        unsigned long long base = 0;
+        if (lane_id() == 0) base = atomicAdd(rs.cursor, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        __syncwarp();
+        if (base + n <= rs.cap)
+            for (uint32_t i = lane_id(); i < n; i += 32) {
+                out[base + i] = pairs[i];
+                out_cnt[base + i] = counts[i];
+            }
+        __syncwarp();
+        n = 0;
+    }
+    // warp-collective: the lanes with `have` add one group each
+    __device__ __forceinline__ void add(bool have, uint32_t xv, uint32_t zv, uint32_t cnt) {
+        const uint32_t b = __ballot_sync(0xffffffffu, have);
+        if (!b) return;
+        if (n + __popc(b) > cap) flush();
+        if (have) {
+            const uint32_t pos = n + __popc(b & lanemask_lt());
+            pairs[pos] = make_uint2(xv, zv);
+            counts[pos] = cnt;
+        }
+        n += __popc(b);
+        __syncwarp();
+    }
+};
+
+// Per-warp shared memory of the COUNT warp classes: 2^(warp_lg+1) map
+// words, then `stage` staged groups (3 words each).
+__host__ __device__ constexpr size_t agg_warp_words(uint32_t warp_lg, uint32_t stage) {
+    return ((size_t)2 << warp_lg) + 3 * (size_t)stage;
+}
+
+static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRows L, uint32_t warp_lg,
+                                                           uint32_t stage) {
     extern __shared__ uint32_t smem[];
     __shared__ RowCtx s_c[8];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = lane_id();
-    uint32_t* keys = smem + ((size_t)wib << (warp_lg + 1));
+    uint32_t* keys = smem + (size_t)wib * agg_warp_words(warp_lg, stage);
     uint32_t* vals = keys + (1u << warp_lg);
+    GroupStage gs{reinterpret_cast<uint2*>(keys + (2u << warp_lg)), keys + (2u << warp_lg) + 2 * stage, nullptr,
+                  nullptr, Reserve{nullptr, 0}, stage};
+    uint32_t cur_q = 0xFFFFFFFFu;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         uint32_t x = 0, qi = 0;
-        if (lane == 0) {
-            qi = query_of_row(Q, L.list[ri], &x);
-            s_c[wib] = Q.rc[qi];
-        }
+        if (lane == 0) qi = query_of_row(Q, L.list[ri], &x);
         qi = __shfl_sync(0xffffffffu, qi, 0);
         x = __shfl_sync(0xffffffffu, x, 0);
-        __syncwarp();
+        if (qi != cur_q) {
+            gs.flush();
+            __syncwarp();
+            if (lane == 0) s_c[wib] = Q.rc[qi];
+            __syncwarp();
+            gs.rs = Q.rs[qi];
+            gs.out = s_c[wib].out;
+            gs.out_cnt = Q.qin[qi].out_cnt;
+            cur_q = qi;
+        }
         const RowCtx& c = s_c[wib];
         const uint32_t u = c.ucap[x];
-        const Reserve rs = Q.rs[qi];
         const uint32_t xv = c.id2x[x];
-        unsigned long long* oc = Q.qin[qi].out_cnt;
         NullSink sink;
         if (use_row_counters(c.m, u, warp_lg + 1)) {
             for (uint32_t s = lane; s < c.m; s += 32) keys[s] = 0;
@@ -502,7 +592,7 @@ static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRo
             for (uint32_t sb = 0; sb < c.m; sb += 32) {
                 const uint32_t z = sb + lane;
                 const uint32_t v = z < c.m ? keys[z] : 0u;
-                emit_groups(c, rs, oc, v != 0, xv, v ? __ldg(&c.id2z[z]) : 0u, v);
+                gs.add(v != 0, xv, v ? __ldg(&c.id2z[z]) : 0u, v);
             }
             __syncwarp();
             continue;
@@ -520,10 +610,11 @@ static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRo
         for (uint32_t sb = 0; sb < (1u << lg); sb += 32) {
             const uint32_t key = keys[sb + lane];
             const bool have = key != kEmpty32;
-            emit_groups(c, rs, oc, have, xv, have ? __ldg(&c.id2z[key]) : 0u, have ? vals[sb + lane] : 0u);
+            gs.add(have, xv, have ? __ldg(&c.id2z[key]) : 0u, have ? vals[sb + lane] : 0u);
         }
         __syncwarp();
     }
+    gs.flush();
 }
 
 static __global__ void __launch_bounds__(256) k_b_agg_block(QueryPools Q, BatchRows L, uint32_t block_lg) {

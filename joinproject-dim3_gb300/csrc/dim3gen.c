@@ -146,6 +146,31 @@ int dim3gen_zipf_side(uint64_t n, uint32_t dom_a, uint32_t dom_b, double s, uint
     return 0;
 }
 
+/* One relation of a served set: first column uniform in [0, dom_a); y rank
+ * Zipf(s) over 2^dom_b_log2 ranks, mapped to a B value through this
+ * relation's own bijection rank -> (mul * rank + add) mod 2^dom_b_log2 (mul
+ * odd) and rank_value, so relations share the B domain but not the order of
+ * their heavy values.  Duplicates are kept. */
+int dim3gen_serve_relation(uint64_t n, uint32_t dom_a, uint32_t dom_b_log2, double s, uint32_t mul, uint32_t add,
+                           uint64_t seed, uint32_t* out) {
+    zipf_t z;
+    const uint32_t dom_b = 1u << dom_b_log2, mask = dom_b - 1;
+    if (zipf_init(&z, dom_b, s)) return -1;
+    mul |= 1u;
+    uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < (int64_t)nchunks; c++) {
+        uint64_t st = stream_seed(seed, (uint64_t)c);
+        uint64_t i0 = (uint64_t)c * CHUNK, i1 = i0 + CHUNK < n ? i0 + CHUNK : n;
+        for (uint64_t i = i0; i < i1; i++) {
+            out[2 * i] = below(&st, dom_a);
+            out[2 * i + 1] = dim3gen_rank_value((mul * zipf_draw(&z, &st) + add) & mask);
+        }
+    }
+    free(z.cdf);
+    return 0;
+}
+
 /* ---------------------------------------------------- Chung-Lu graph */
 /* Undirected Chung-Lu power-law graph: vertex i has weight
  * (i+1)^(-1/(beta-1)) scaled to mean degree 2M/n and capped at sqrt(sum w);

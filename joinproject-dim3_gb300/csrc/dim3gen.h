@@ -18,6 +18,9 @@ uint64_t dim3gen_chung_lu(uint32_t n, double beta, uint64_t M, uint64_t seed, ui
 void dim3gen_batch_params(uint64_t seed, uint32_t q, double n_lo, double n_hi, double s_lo, double s_hi,
                           double d_lo, double d_hi, uint64_t* n_out, double* s_out, uint32_t* dom_out);
 uint32_t dim3gen_rank_value(uint32_t rank);
+/* One relation of a served set (see dim3gen.c). */
+int dim3gen_serve_relation(uint64_t n, uint32_t dom_a, uint32_t dom_b_log2, double s, uint32_t mul, uint32_t add,
+                           uint64_t seed, uint32_t* out);
 double dim3gen_det_pow(double b, double e);
 #ifdef __cplusplus
 }

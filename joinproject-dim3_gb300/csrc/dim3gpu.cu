@@ -85,8 +85,8 @@ constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counter
 struct Scalars {
     unsigned long long nx, ny, nz, nkept, total, outj;
     unsigned long long cursor;     // single-pass output cursor
-    unsigned long long nrows[5];   // rows per class (index = class)
-    unsigned long long outj_cls[5];  // candidates per class (index = class)
+    unsigned long long nrows[6];   // rows per class (index = class)
+    unsigned long long outj_cls[6];  // candidates per class (index = class)
     unsigned long long cursor_at[3]; // single-pass cursor after the bitmap / block / warp kernel
     unsigned int err;
     unsigned int next_row[4];      // dynamic row counters of the CTA classes
@@ -313,7 +313,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* Zq = ws_get<uint32_t>(c, nq);
     uint32_t* ucap = ws_get<uint32_t>(c, n);
     uint8_t* cls = ws_get<uint8_t>(c, n);
-    uint32_t* lists = ws_get<uint32_t>(c, (uint64_t)3 * n);
+    uint32_t* lists = ws_get<uint32_t>(c, (uint64_t)4 * n);
     uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
     uint64_t* bsum2 = ws_get<uint64_t>(c, scan_storage((nyt > n ? nyt : n) + 1));
@@ -352,17 +352,21 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     rc.err = &sc->err;
     const uint32_t cap_w = 1u << (c->prm.warp_lg - 1);
     const uint32_t cap_b = 1u << (c->prm.block_lg - 1);
-    k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, ucap, cls,
+    // tiny rows get their own warp launch in the single pass only
+    const bool tiny = jp.single_pass && !jp.aggregate && !jp.count_only;
+    k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, tiny, ucap, cls,
                                                                 &sc->outj, sc->outj_cls);
     CHECK_LAUNCH();
     uint32_t* list_w = lists;
     uint32_t* list_b = lists + n;
     uint32_t* list_m = lists + 2 * (uint64_t)n;
+    uint32_t* list_t = lists + 3 * (uint64_t)n;
     SCAN(ClassSrc{cls, 1}, ListDst{list_w, nullptr}, n, bsum2, &sc->nrows[1]);
     SCAN(ClassSrc{cls, 2}, ListDst{list_b, nullptr}, n, bsum2, &sc->nrows[2]);
     // bitmap rows: class 4 (huge) first, then class 3
     SCAN(ClassSrc{cls, 4}, ListDst{list_m, nullptr}, n, bsum2, &sc->nrows[4]);
     SCAN(ClassSrc{cls, 3}, ListDst{list_m, &sc->nrows[4]}, n, bsum2, &sc->nrows[3]);
+    if (tiny) SCAN(ClassSrc{cls, 5}, ListDst{list_t, nullptr}, n, bsum2, &sc->nrows[5]);
     CU(cudaMemsetAsync(cnt, 0, ((uint64_t)n + 1) * 4, st));
     CU(cudaEventRecord(c->ev[2], st));
 
@@ -392,8 +396,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         const uint32_t bm_words = (uint32_t)(smem_m / 4);
         const size_t ss_m = smem_m + (size_t)(blk_m / 32) * kStage * 4;
         const size_t ss_b = smem_b + (size_t)(blk_b / 32) * kStage * 4;
-        const uint32_t wps = warps_per_cta(((size_t)(1u << c->prm.warp_lg) + kStage) * 4);
-        const size_t ss_w = (size_t)wps * ((1u << c->prm.warp_lg) + kStage) * 4;
+        const uint32_t wps = warps_per_cta(warp_row_words(c->prm.warp_lg, kStage) * 4);
+        const size_t ss_w = (size_t)wps * warp_row_words(c->prm.warp_lg, kStage) * 4;
+        const uint32_t wpt = warps_per_cta(warp_row_words(kTinyLg, kTinyStage) * 4);
+        const size_t ss_t = (size_t)wpt * warp_row_words(kTinyLg, kTinyStage) * 4;
         k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3, L.n4,
                                                                                          bm_words);
         CHECK_LAUNCH();
@@ -405,7 +411,11 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CU(cudaEventRecord(c->evc[6], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[1], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
         k_single_warp<<<resident_grid(k_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(rc, rs, L.w, L.nw,
-                                                                                           c->prm.warp_lg);
+                                                                                           c->prm.warp_lg, kStage);
+        CHECK_LAUNCH();
+        k_single_warp<<<resident_grid(k_single_warp, 32 * wpt, ss_t, sm), 32 * wpt, ss_t, st>>>(rc, rs, list_t,
+                                                                                           &sc->nrows[5], kTinyLg,
+                                                                                           kTinyStage);
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[7], st));
         CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
@@ -418,12 +428,12 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         S.n_out_cls[1] = c->h_sc->cursor_at[1] - c->h_sc->cursor_at[0];
         S.n_out_cls[2] = total - c->h_sc->cursor_at[1];
         S.n_out = total;
-        S.rows_warp = (uint32_t)c->h_sc->nrows[1];
+        S.rows_warp = (uint32_t)(c->h_sc->nrows[1] + c->h_sc->nrows[5]);
         S.rows_block = (uint32_t)c->h_sc->nrows[2];
         S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
         S.out_j_cls[0] = c->h_sc->outj_cls[3] + c->h_sc->outj_cls[4];
         S.out_j_cls[1] = c->h_sc->outj_cls[2];
-        S.out_j_cls[2] = c->h_sc->outj_cls[1];
+        S.out_j_cls[2] = c->h_sc->outj_cls[1] + c->h_sc->outj_cls[5];
         *n_out = total;
         float a, b, e;
         cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);

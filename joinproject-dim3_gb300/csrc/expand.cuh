@@ -22,6 +22,10 @@ namespace dim3g {
 constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
 constexpr uint32_t kHugeRow = 1u << 16;
 constexpr uint32_t kWarpWorkMax = 1u << 14;  // candidates a single warp takes alone
+// Tiny rows (few distinct z, few candidates) run in the warp kernel with a
+// 2^kTinyLg-slot table and a kTinyStage-pair stage: about 3 KB of shared
+// memory per warp, so the latency-bound row walk runs at full occupancy.
+constexpr uint32_t kTinyU = 128, kTinyW = 4096, kTinyLg = 8, kTinyStage = 256;
 
 // A hash-class row dedups with a bitmap over the whole z domain instead of
 // a hash set when that bitmap fits the kernel's table memory (2^slots_lg
@@ -31,12 +35,15 @@ constexpr uint32_t kWarpWorkMax = 1u << 14;  // candidates a single warp takes a
 __device__ __forceinline__ bool use_row_bitmap(uint32_t m, uint32_t u, uint32_t slots_lg) {
     return (uint64_t)m <= (32ull << slots_lg) && (uint64_t)m <= 32ull * u;
 }
-// Row class from its candidates w and u = min(w, m): 1 (one warp) for few
-// distinct z and few candidates, 2 (one CTA, hash set or bitmap) up to
-// cap_b distinct, 3 / 4 (one CTA, z-tile bitmaps; 4 = huge, scheduled
+// Row class from its candidates w and u = min(w, m): 5 (one warp, small
+// table; only where the caller runs that kernel) for tiny rows, 1 (one warp)
+// for few distinct z and few candidates, 2 (one CTA, hash set or bitmap) up
+// to cap_b distinct, 3 / 4 (one CTA, z-tile bitmaps; 4 = huge, scheduled
 // first) beyond; 0 for an empty row.
-__device__ __forceinline__ uint32_t row_class(unsigned long long w, uint32_t u, uint32_t cap_w, uint32_t cap_b) {
+__device__ __forceinline__ uint32_t row_class(unsigned long long w, uint32_t u, uint32_t cap_w, uint32_t cap_b,
+                                              bool tiny) {
     if (u == 0) return 0;
+    if (tiny && u <= kTinyU && w <= kTinyW) return 5;
     if (u <= cap_w && w <= kWarpWorkMax) return 1;
     if (u <= cap_b) return 2;
     return u <= kHugeRow ? 3 : 4;
@@ -95,17 +102,25 @@ __device__ __forceinline__ bool smem_set_insert(uint32_t* tab, uint32_t lg, uint
 #ifndef DIM3G_MIN_PIECE
 #define DIM3G_MIN_PIECE 256
 #endif
+#ifndef DIM3G_FLAT_AVG
+#define DIM3G_FLAT_AVG 96
+#endif
 constexpr uint32_t kUnroll = DIM3G_UNROLL;
 constexpr uint32_t kMinPiece = DIM3G_MIN_PIECE;
+// A chunk whose segments average fewer candidates than this is gathered
+// across segment boundaries (see warp_expand).
+constexpr uint32_t kFlatAvgMax = DIM3G_FLAT_AVG;
 
 // Warp-level expansion of the candidates of R entries [e0, e1) over S tiles
 // [t0, t1).  Entries are taken 32 at a time; a warp prefix sum over their S
 // segment lengths flattens the chunk's candidates into [0, total), which is
 // cut into a power-of-two number (<= nparts) of contiguous pieces of at least
-// kMinPiece candidates; the calling warp takes piece `part`.  It finds the
-// segment holding its first candidate with one ballot over the lanes'
-// inclusive prefixes, then walks the segments overlapping its piece, the
-// lanes striding each segment kUnroll x 32 candidates at a time.
+// kMinPiece candidates; the calling warp takes piece `part`.  When the
+// chunk's segments are short on average it gathers its piece across segment
+// boundaries (each lane looks up its candidate's segment); otherwise it
+// finds the segment holding its first candidate with one ballot over the
+// lanes' inclusive prefixes, then walks the segments overlapping its piece,
+// the lanes striding each segment kUnroll x 32 candidates at a time.
 //   set.insert(z, active) -> bool   per lane (false when !active)
 //   sink.take(b[], v[])             warp-collective once per group: b[u] is
 //                                   the ballot of first insertions of step u;
@@ -138,6 +153,36 @@ __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32
         const uint32_t p1 = min(p0 + piece, total);
         if (p0 >= p1) continue;
         const uint32_t excl = incl - len;
+        // Many short segments: gather across segment boundaries.  Each lane
+        // finds the segment of its candidate c (the number of lanes with
+        // incl <= c; incl is nondecreasing over lanes) by a 5-step binary
+        // search over the lanes' prefixes, so one group of kUnroll x 32
+        // loads covers many segments with a single memory latency.
+        const uint32_t nseg = __popc(__ballot_sync(0xffffffffu, len != 0));
+        if (total < kFlatAvgMax * nseg) {
+            for (uint32_t cb = p0; cb < p1; cb += 32 * kUnroll) {
+                uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+                for (uint32_t u = 0; u < kUnroll; u++) {
+                    const uint32_t cc = cb + u * 32 + lane;
+                    const bool act = cc < p1;
+                    const uint32_t ci = act ? cc : p0;  // idle lanes search a valid index
+                    uint32_t k = 0;
+#pragma unroll
+                    for (uint32_t step = 16; step >= 1; step >>= 1)
+                        if (__shfl_sync(0xffffffffu, incl, k + step - 1) <= ci) k += step;
+                    const uint32_t j = __shfl_sync(0xffffffffu, s0, k) + (ci - __shfl_sync(0xffffffffu, excl, k));
+                    z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
+                    if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
+                }
+                uint32_t b[kUnroll];
+#pragma unroll
+                for (uint32_t u = 0; u < kUnroll; u++)
+                    b[u] = (cb + u * 32 < p1) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
+                sink.take(b, v);
+            }
+            continue;
+        }
         // first segment holding candidate p0: lanes with incl <= p0 form a prefix
         for (uint32_t k = __popc(__ballot_sync(0xffffffffu, incl <= p0)); k < 32; k++) {
             const uint32_t kex = __shfl_sync(0xffffffffu, excl, k);
@@ -389,13 +434,13 @@ static __global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uin
 // the row class (0: empty).  One warp per row.  With check_range set
 // (join-aggregate, 32-bit per-group counters) a row of 2^32 or more
 // candidates raises kErrCountRange.
-static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range,
+static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range, bool tiny,
                            uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj,
                            unsigned long long* outj_cls) {
     const uint32_t lane = lane_id();
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long acc = 0, acc_cls[5] = {0, 0, 0, 0, 0};
+    unsigned long long acc = 0, acc_cls[6] = {0, 0, 0, 0, 0, 0};
     for (uint64_t x = gw; x < n; x += nwarps) {
         uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
         unsigned long long w = 0;
@@ -407,18 +452,18 @@ static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t
         if (lane == 0) {
             uint32_t u = (uint32_t)(w < c.m ? w : c.m);
             ucap[x] = u;
-            const uint32_t k = row_class(w, u, cap_w, cap_b);
+            const uint32_t k = row_class(w, u, cap_w, cap_b, tiny);
             cls[x] = (uint8_t)k;
             if (check_range && w >= 0xFFFFFFFFull) raise_error(c.err, kErrCountRange);
             acc += w;
 #pragma unroll
-            for (uint32_t j = 1; j < 5; j++) acc_cls[j] += (j == k) ? w : 0ull;
+            for (uint32_t j = 1; j < 6; j++) acc_cls[j] += (j == k) ? w : 0ull;
         }
     }
     if (lane == 0 && acc) {
         atomicAdd(outj, acc);
 #pragma unroll
-        for (uint32_t j = 1; j < 5; j++)
+        for (uint32_t j = 1; j < 6; j++)
             if (acc_cls[j]) atomicAdd(&outj_cls[j], acc_cls[j]);
     }
 }

@@ -61,14 +61,58 @@ struct StageSink {
     }
 };
 
+// As StageSink, but staging (x value, z value) pairs, so a warp keeps one
+// buffer across the many small rows it takes and reserves output once per
+// kStage pairs instead of once per row (millions of rows of a few pairs
+// each would otherwise serialise on the cursor).  The owner sets xv per row
+// and flushes when it changes cursor and at the end.
+struct PairStageSink {
+    static constexpr bool kValues = true;
+    uint2* stage;  // this warp's buffer of `cap` pairs
+    uint2* out;
+    Reserve rs;
+    uint32_t xv;
+    uint32_t cap;  // staged pairs the buffer holds (at least 32 * kUnroll)
+    uint32_t n = 0;
+
+    __device__ __forceinline__ void flush() {
+        if (n == 0) return;
+        unsigned long long base = 0;
+        if (lane_id() == 0) base = atomicAdd(rs.cursor, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        __syncwarp();
+        if (base + n <= rs.cap)
+            for (uint32_t i = lane_id(); i < n; i += 32) st_stream(&out[base + i], stage[i]);
+        __syncwarp();
+        n = 0;
+    }
+
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&b)[N], const uint32_t (&v)[N]) {
+        uint32_t tot = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < N; u++) tot += __popc(b[u]);
+        if (tot == 0) return;
+        if (n + tot > cap) flush();
+        const uint32_t lt = lanemask_lt();
+        uint32_t pos = n;
+#pragma unroll
+        for (uint32_t u = 0; u < N; u++) {
+            if (b[u] & (1u << lane_id())) stage[pos + __popc(b[u] & lt)] = make_uint2(xv, v[u]);
+            pos += __popc(b[u]);
+        }
+        n += tot;
+    }
+};
+
 // ---- row bodies (shared by the one-join kernels below and the many-query
 // kernels of batch.cuh)
 
-// Class 1: the calling warp expands row x; its own 2^warp_lg-word table
-// (hash set, or a whole-domain bitmap when use_row_bitmap) and kStage-entry
-// staging buffer.
-__device__ __forceinline__ void single_warp_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* tab,
-                                                uint32_t* stage, uint32_t warp_lg) {
+// Class 1: the calling warp expands row x with its own 2^warp_lg-word table
+// (hash set, or a whole-domain bitmap when use_row_bitmap) into the warp's
+// pair sink, which stays open across the warp's rows.
+__device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uint32_t* tab, PairStageSink& sink,
+                                                uint32_t warp_lg) {
     const uint32_t lane = lane_id();
     const uint32_t u = c.ucap[x];
     const bool bm = use_row_bitmap(c.m, u, warp_lg);
@@ -78,7 +122,7 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, const Reserve& 
     const uint32_t fill = bm ? 0u : kEmpty32;
     for (uint32_t s = lane; s < nclr; s += 32) tab[s] = fill;
     __syncwarp();
-    StageSink sink{stage, c.out, rs, c.id2x[x]};
+    sink.xv = c.id2x[x];
     if (bm) {
         TileBitmap set{tab, 0};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
@@ -86,7 +130,7 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, const Reserve& 
         HashSet set{tab, lg, c.err};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
     }
-    sink.flush();
+    __syncwarp();
 }
 
 // Class 2: the whole CTA expands row x; a 2^block_lg-word table (hash set or
@@ -140,17 +184,24 @@ __device__ __forceinline__ void single_bitmap_row(const RowCtx& c, const Reserve
 
 // ---- one join
 
-// Class 1: one warp per row; per warp 2^warp_lg table words then kStage
-// staging entries.
+// Shared memory per warp of the warp classes: 2^warp_lg table words, then
+// `stage` staged pairs.
+__host__ __device__ constexpr size_t warp_row_words(uint32_t warp_lg, uint32_t stage) {
+    return ((size_t)1 << warp_lg) + 2 * (size_t)stage;
+}
+
+// Classes 1 and 5 (tiny): one warp per row.
 static __global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
                                                             const unsigned long long* __restrict__ nrows_p,
-                                                            uint32_t warp_lg) {
+                                                            uint32_t warp_lg, uint32_t stage) {
     extern __shared__ uint32_t smem[];
     const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5;
-    uint32_t* tab = smem + (size_t)wib * ((1u << warp_lg) + kStage);
+    uint32_t* tab = smem + (size_t)wib * warp_row_words(warp_lg, stage);
+    PairStageSink sink{reinterpret_cast<uint2*>(tab + (1u << warp_lg)), c.out, rs, 0, stage};
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw)
-        single_warp_row(c, rs, rows[ri], tab, tab + (1u << warp_lg), warp_lg);
+        single_warp_row(c, rows[ri], tab, sink, warp_lg);
+    sink.flush();
 }
 
 // Class 2: one CTA per row; 2^block_lg table words, then one staging buffer

@@ -71,7 +71,21 @@ EXPORTS = [
     "dim3g_join_project_noalloc",
     "dim3g_relset_create", "dim3g_relset_destroy", "dim3g_relset_bytes", "dim3g_relset_join",
     "dim3g_batch_create", "dim3g_batch_run", "dim3g_batch_info", "dim3g_batch_destroy",
+    "dim3g_relset_pair_outj", "dim3g_server_create", "dim3g_server_submit", "dim3g_server_wait",
+    "dim3g_server_release", "dim3g_server_stats", "dim3g_server_destroy",
 ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("ticket", ctypes.c_uint64), ("status", ctypes.c_int32), ("swapped", ctypes.c_uint32),
+        ("n_out", ctypes.c_uint64), ("out_j", ctypes.c_uint64), ("d_out", ctypes.c_void_p), ("d_cnt", ctypes.c_void_p),
+        ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double), ("t_done", ctypes.c_double),
+        ("pass_size", ctypes.c_uint32), ("lane", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 OP_PROJECT, OP_COUNT = 0, 1
 
@@ -140,6 +154,14 @@ def load(path=LIB_PATH):
     L.dim3g_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_float), _u64p, _u64p]
     L.dim3g_batch_destroy.argtypes = [vp]
     L.dim3g_batch_destroy.restype = None
+    L.dim3g_relset_pair_outj.argtypes = [vp, _u64p]
+    L.dim3g_server_create.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.dim3g_server_submit.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _u64p]
+    L.dim3g_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(Result)]
+    L.dim3g_server_release.argtypes = [vp, ctypes.c_uint64]
+    L.dim3g_server_stats.argtypes = [vp, _u64p, _u64p, _u64p, _u64p]
+    L.dim3g_server_destroy.argtypes = [vp]
+    L.dim3g_server_destroy.restype = None
     _lib = L
     return L
 
@@ -305,6 +327,12 @@ class RelSet:
     def bytes(self):
         return self.L.dim3g_relset_bytes(self.h)
 
+    def pair_outj(self):
+        n = len(self._keep)
+        m = np.zeros(n * n, dtype=np.uint64)
+        self.ctx._check(self.L.dim3g_relset_pair_outj(self.h, m.ctypes.data_as(_u64p)))
+        return m.reshape(n, n)
+
     def join(self, specs, check=True):
         """Runs the queries in one pass; returns per-query results (and
         raises on the first failing status when check is set)."""
@@ -324,6 +352,73 @@ class RelSet:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching server over a RelSet (lanes run query passes on
+    their own streams; outputs stay on the device until released)."""
+
+    def __init__(self, relset, lanes=2, max_batch=64, budget_bytes=120 << 30):
+        self.relset, self.ctx, self.L = relset, relset.ctx, relset.L
+        self.h = ctypes.c_void_p()
+        self.ctx._check(self.L.dim3g_server_create(relset.h, lanes, max_batch, budget_bytes, ctypes.byref(self.h)))
+
+    def submit(self, r, s, op=OP_PROJECT):
+        t = ctypes.c_uint64()
+        self.ctx._check(self.L.dim3g_server_submit(self.h, r, s, op, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket):
+        res = Result()
+        self.ctx._check(self.L.dim3g_server_wait(self.h, ticket, ctypes.byref(res)))
+        return res.as_dict()
+
+    def release(self, ticket):
+        self.ctx._check(self.L.dim3g_server_release(self.h, ticket))
+
+    def stats(self):
+        v = [ctypes.c_uint64() for _ in range(4)]
+        self.ctx._check(self.L.dim3g_server_stats(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["completed", "passes", "reserved_bytes", "output_budget"], [x.value for x in v]))
+
+    def close(self):
+        if self.h:
+            self.L.dim3g_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DeviceArray:
+    """A device address viewed through __cuda_array_interface__ (zero copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2, "strides": None}
+
+
+def device_tensor(ptr, shape, typestr="<i4"):
+    """torch tensor over device memory the library owns (valid until that
+    memory is released)."""
+    import torch
+    return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device="cuda")
+
+
+def device_pairs(d_out, n):
+    """n pairs at a device address as a (n, 2) uint32 host array."""
+    if n == 0:
+        return np.empty((0, 2), dtype=np.uint32)
+    return device_tensor(d_out, (n, 2), "<i4").cpu().numpy().view(np.uint32)
+
+
+def device_u64(d_ptr, n):
+    if n == 0:
+        return np.empty(0, dtype=np.uint64)
+    return device_tensor(d_ptr, (n,), "<i8").cpu().numpy().view(np.uint64)
 
 
 class Batch:
@@ -423,6 +518,8 @@ def gen():
         G.dim3gen_batch_params.argtypes = [ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_double] * 6 + [
             _u64p, ctypes.POINTER(ctypes.c_double), _u32p]
         G.dim3gen_rank_value.argtypes = [ctypes.c_uint32]
+        G.dim3gen_serve_relation.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                                             ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _u32p]
         G.dim3gen_rank_value.restype = ctypes.c_uint32
         _gen = G
     return _gen
@@ -499,6 +596,31 @@ def batch_relations(params):
     over dom ranks, the same rank -> value map on both sides."""
     return [(zipf_side(p["nR"], p["dom"], p["dom"], p["s"], p["seed_R"]),
              zipf_side(p["nS"], p["dom"], p["dom"], p["s"], p["seed_S"])) for p in params]
+
+
+def serve_params(n_rel=64, seed=5, n_lo=1e6, n_hi=16e6, alpha_lo=1.8, alpha_hi=2.5, dom_b_log2=18, scale=1.0):
+    """Relations of the served set: |R| log-uniform in [n_lo, n_hi] (times
+    scale); B-degree power-law exponent alpha uniform in [alpha_lo,
+    alpha_hi], drawn as Zipf ranks with s = 1 / (alpha - 1) over a shared
+    domain of 2^dom_b_log2 B values, each relation with its own rank -> value
+    bijection; dom(A) = |R| / 4."""
+    out = []
+    for i in range(n_rel):
+        rng = np.random.default_rng([seed, i])
+        n = max(1, int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))) * scale))
+        alpha = float(rng.uniform(alpha_lo, alpha_hi))
+        out.append({"n": n, "alpha": alpha, "s": 1.0 / (alpha - 1.0), "dom_a": max(1024, n // 4),
+                    "dom_b_log2": dom_b_log2, "mul": int(rng.integers(0, 1 << 31)) * 2 + 1,
+                    "add": int(rng.integers(0, 1 << 31)), "seed": (seed << 40) + i})
+    return out
+
+
+def serve_relation(p):
+    out = np.empty((p["n"], 2), dtype=np.uint32)
+    if gen().dim3gen_serve_relation(p["n"], p["dom_a"], p["dom_b_log2"], p["s"], p["mul"] & 0xFFFFFFFF,
+                                    p["add"] & 0xFFFFFFFF, p["seed"], out.ctypes.data_as(_u32p)) != 0:
+        raise MemoryError("serve generator failed")
+    return out
 
 
 def workload(name, scale=1.0):
