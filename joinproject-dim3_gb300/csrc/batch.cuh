@@ -469,13 +469,19 @@ static __global__ void __launch_bounds__(256) k_b_single_warp(QueryPools Q, Batc
     // the warp's pairs are staged across its rows and flushed when the
     // query (cursor and output) changes
     PairStageSink sink{reinterpret_cast<uint2*>(tab + (1u << warp_lg)), nullptr, Reserve{nullptr, 0}, 0, stage};
-    uint32_t cur_q = 0xFFFFFFFFu;
+    uint32_t cur_q = 0xFFFFFFFFu, q_lo = 1, q_hi = 0;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
-        uint32_t x = 0, qi = 0;
-        if (lane == 0) qi = query_of_row(Q, L.list[ri], &x);
-        qi = __shfl_sync(0xffffffffu, qi, 0);
-        x = __shfl_sync(0xffffffffu, x, 0);
+        // rows of one query are contiguous in the list: look the query up
+        // only when the row leaves the current query's row range
+        const uint32_t g = L.list[ri];
+        uint32_t qi = cur_q;
+        if (g < q_lo || g >= q_hi) {
+            qi = seg_find(Q.qrow_off, Q.nq, g);
+            q_lo = (uint32_t)Q.qrow_off[qi];
+            q_hi = (uint32_t)Q.qrow_off[qi + 1];
+        }
+        const uint32_t x = g - q_lo;
         if (qi != cur_q) {
             sink.flush();
             __syncwarp();
@@ -562,13 +568,19 @@ static __global__ void __launch_bounds__(256) k_b_agg_warp(QueryPools Q, BatchRo
     uint32_t* vals = keys + (1u << warp_lg);
     GroupStage gs{reinterpret_cast<uint2*>(keys + (2u << warp_lg)), keys + (2u << warp_lg) + 2 * stage, nullptr,
                   nullptr, Reserve{nullptr, 0}, stage};
-    uint32_t cur_q = 0xFFFFFFFFu;
+    uint32_t cur_q = 0xFFFFFFFFu, q_lo = 1, q_hi = 0;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
-        uint32_t x = 0, qi = 0;
-        if (lane == 0) qi = query_of_row(Q, L.list[ri], &x);
-        qi = __shfl_sync(0xffffffffu, qi, 0);
-        x = __shfl_sync(0xffffffffu, x, 0);
+        // rows of one query are contiguous in the list: look the query up
+        // only when the row leaves the current query's row range
+        const uint32_t g = L.list[ri];
+        uint32_t qi = cur_q;
+        if (g < q_lo || g >= q_hi) {
+            qi = seg_find(Q.qrow_off, Q.nq, g);
+            q_lo = (uint32_t)Q.qrow_off[qi];
+            q_hi = (uint32_t)Q.qrow_off[qi + 1];
+        }
+        const uint32_t x = g - q_lo;
         if (qi != cur_q) {
             gs.flush();
             __syncwarp();
