@@ -111,6 +111,29 @@ int dim3g_join_count(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const ui
 int dim3g_join_count_device(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
                             uint32_t* d_out_xz, uint64_t* d_out_cnt, uint64_t capacity, uint64_t* n_out);
 
+/* ---- summaries: results too large to materialise ----------------------
+ * No counterpart in the reference.  Nothing is written to an output; the
+ * pairs (or groups) are summarised per A-tile, t(a) = murmur3 fmix32(a) &
+ * (tiles - 1) of the pair's first value a:
+ *   groups     distinct pairs of the tile
+ *   count_sum  sum of the groups' counts (COUNT; the tile's OUT_J), or
+ *              groups (join-project)
+ *   hash       sum mod 2^64 of pair_hash(a, c) (join-project) or of
+ *              mix64(pair_hash(a, c) + count) (COUNT), pair_hash = mix64 =
+ *              the splitmix64 finaliser of a << 32 | c
+ * Only tiles in [tile_lo, tile_hi) are computed (rows of other tiles are
+ * skipped), so a join too large for one call is covered in slices, and a
+ * slice can be checked on the CPU from its rows of R alone.  tiles: a power
+ * of two <= 2^20; out: host array of `tiles` entries (others zero).  Device
+ * inputs as for dim3g_join_project_device. */
+typedef struct {
+    uint64_t groups, count_sum, hash;
+} dim3g_tile_summary;
+int dim3g_join_project_summary(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
+                               uint32_t tiles, uint32_t tile_lo, uint32_t tile_hi, dim3g_tile_summary* out);
+int dim3g_join_count_summary(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
+                             uint32_t tiles, uint32_t tile_lo, uint32_t tile_hi, dim3g_tile_summary* out);
+
 /* ---- allocation-free join-project ------------------------------------
  * No counterpart in the reference.  For callers that must not allocate
  * device memory where they need the join: code under a custom or
@@ -240,6 +263,33 @@ int dim3g_batch_run(dim3g_batch* b, dim3g_query* q);
  * per run, device bytes held. */
 int dim3g_batch_info(const dim3g_batch* b, float* ms_last, uint64_t* launches_per_run, uint64_t* device_bytes);
 void dim3g_batch_destroy(dim3g_batch* b);
+
+/* ---- autotuner ----------------------------------------------------------
+ * Replaces server_parameter_estimator.cpp:77-269 and the cost models that
+ * consume its constants (dim3.hpp:42-186): instead of machine constants fed
+ * to a model, the join is timed on the caller's device-resident input under
+ * candidate settings of the knobs that set the row classes' thresholds and
+ * tile shapes (tile_bits_log2, block_threads, block_slots_log2,
+ * warp_slots_log2), by coordinate descent from the context's current
+ * settings (always a trial), and the fastest are applied to the context.
+ * max_trials bounds the joins run (0: no bound). */
+typedef struct {
+    int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2;
+    float ms;          /* best measured device ms of one join */
+    float ms_default;  /* the starting settings' ms */
+    uint32_t trials;   /* settings timed */
+} dim3g_tuning;
+int dim3g_autotune(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
+                   uint32_t max_trials, dim3g_tuning* out);
+int dim3g_tuning_apply(dim3g_ctx* ctx, const dim3g_tuning* t);
+/* Shape signature of a workload ("p<lg |P|>_z<lg |z|>_w<lg candidates per
+ * row>"), from one count pass; key_len >= 32. */
+int dim3g_tuning_key(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS, char* key,
+                     uint64_t key_len);
+/* Text cache of tunings by key (one line each; the last line of a key wins).
+ * Host-only; DIM3G_ERR_INVALID when the file or key is absent. */
+int dim3g_tuning_save(const char* path, const char* key, const dim3g_tuning* t);
+int dim3g_tuning_load(const char* path, const char* key, dim3g_tuning* out);
 
 /* ---- L+S mapper -----------------------------------------------------
  * Replaces LS_mapper<T,H,Tcounter> (Include/L+S_mapper.hpp:11-160): a GPU

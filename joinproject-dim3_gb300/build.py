@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 GPU_SO = os.path.join(HERE, "libdim3gpu.so")
 GEN_SO = os.path.join(HERE, "libdim3gen.so")
-GPU_TUS = ["dim3gpu.cu", "batch.cu", "noalloc.cu"]
+GPU_TUS = ["dim3gpu.cu", "batch.cu", "tune.cu", "noalloc.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC"]

@@ -15,7 +15,33 @@ namespace dim3g {
 
 struct AggOut {
     unsigned long long* cnt;  // one count per output pair
+    SumAcc sum;               // sum.tiles set: summaries instead of output
 };
+
+// Summary emission: per-lane sums over the occupied map slots [s0, s1)
+// (stride 32) or over the nonzero direct counters.
+struct GroupSums {
+    unsigned long long g = 0, cs = 0, h = 0;
+    __device__ __forceinline__ void add(uint32_t xv, uint32_t zv, uint32_t cnt) {
+        g++;
+        cs += cnt;
+        h += group_hash(xv, zv, cnt);
+    }
+};
+__device__ __forceinline__ void sum_map_slots(const RowCtx& c, const uint32_t* keys, const uint32_t* vals,
+                                              uint32_t s0, uint32_t s1, uint32_t xv, GroupSums& gs) {
+    for (uint32_t s = s0 + lane_id(); s < s1; s += 32) {
+        const uint32_t key = keys[s];
+        if (key != kEmpty32) gs.add(xv, __ldg(&c.id2z[key]), vals[s]);
+    }
+}
+__device__ __forceinline__ void sum_counters(const RowCtx& c, const uint32_t* ctr, uint32_t s0, uint32_t s1,
+                                             uint32_t lo, uint32_t xv, GroupSums& gs) {
+    for (uint32_t s = s0 + lane_id(); s < s1; s += 32) {
+        const uint32_t v = ctr[s];
+        if (v) gs.add(xv, __ldg(&c.id2z[lo + s]), v);
+    }
+}
 
 // Shared-memory map slot of z (inserting it if absent).
 __device__ __forceinline__ uint32_t smem_map_slot(uint32_t* keys, uint32_t lg, uint32_t z, uint32_t* err) {
@@ -150,6 +176,7 @@ static __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, co
     for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
         const uint32_t x = rows[ri];
         const uint32_t u = c.ucap[x];
+        const bool sum = ao.sum.tiles != nullptr;
         NullSink sink;
         uint32_t pos = 0;
         if (use_row_counters(c.m, u, warp_lg + 1)) {
@@ -158,7 +185,13 @@ static __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, co
             CountTile set{keys, 0};
             warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
             __syncwarp();
-            emit_counters_warp(c, ao, keys, 0, c.m, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+            if (sum) {
+                GroupSums gs;
+                sum_counters(c, keys, 0, c.m, 0, c.id2x[x], gs);
+                ao.sum.commit(c.id2x[x], gs.g, gs.cs, gs.h);
+            } else {
+                emit_counters_warp(c, ao, keys, 0, c.m, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+            }
             __syncwarp();
             continue;
         }
@@ -172,7 +205,13 @@ static __global__ void __launch_bounds__(256) k_agg_warp(RowCtx c, AggOut ao, co
         CountMap set{keys, vals, lg, c.err};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], 0, 0, 0, c.T, set, sink);
         __syncwarp();
-        emit_map_slots_warp(c, ao, keys, vals, 0, 1u << lg, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+        if (sum) {
+            GroupSums gs;
+            sum_map_slots(c, keys, vals, 0, 1u << lg, c.id2x[x], gs);
+            ao.sum.commit(c.id2x[x], gs.g, gs.cs, gs.h);
+        } else {
+            emit_map_slots_warp(c, ao, keys, vals, 0, 1u << lg, c.id2x[x], c.off[x], c.cnt[x], nullptr, &pos);
+        }
         __syncwarp();
     }
 }
@@ -215,8 +254,16 @@ static __global__ void __launch_bounds__(256) k_agg_block(RowCtx c, AggOut ao, c
         const uint32_t span = direct ? c.m : (1u << lg);
         const uint32_t per = (((span + nw - 1) / nw) + 31) & ~31u;
         const uint32_t s0 = min(span, wib * per), s1 = min(span, s0 + per);
-        if (direct) emit_counters_warp(c, ao, keys, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
-        else emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        if (ao.sum.tiles) {
+            GroupSums gs;
+            if (direct) sum_counters(c, keys, s0, s1, 0, c.id2x[x], gs);
+            else sum_map_slots(c, keys, vals, s0, s1, c.id2x[x], gs);
+            ao.sum.commit(c.id2x[x], gs.g, gs.cs, gs.h);
+        } else if (direct) {
+            emit_counters_warp(c, ao, keys, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        } else {
+            emit_map_slots_warp(c, ao, keys, vals, s0, s1, c.id2x[x], c.off[x], c.cnt[x], &s_pos, nullptr);
+        }
     }
 }
 
@@ -231,8 +278,10 @@ static __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, c
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
     for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
         const uint32_t x = rows[ri];
-        const unsigned long long base = c.off[x];
-        const uint32_t lim = c.cnt[x], xv = c.id2x[x];
+        const bool sum = ao.sum.tiles != nullptr;
+        const unsigned long long base = sum ? 0 : c.off[x];
+        const uint32_t lim = sum ? 0 : c.cnt[x], xv = c.id2x[x];
+        GroupSums gs;
         if (threadIdx.x == 0) s_pos = 0;
         for (uint32_t t = 0; t < c.T; t++) {
             const uint32_t lo = t * c.tile_width;
@@ -243,6 +292,12 @@ static __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, c
             NullSink sink;
             warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
             __syncthreads();
+            if (sum) {
+                for (uint32_t wb = wib * 32; wb < width; wb += nw * 32)
+                    sum_counters(c, ctr, wb, min(width, wb + 32), lo, xv, gs);
+                __syncthreads();
+                continue;
+            }
             // emit the nonzero counters of this tile
             for (uint32_t wb = wib * 32; wb < width; wb += nw * 32) {
                 uint32_t w = wb + lane;
@@ -264,6 +319,7 @@ static __global__ void __launch_bounds__(1024) k_agg_tile(RowCtx c, AggOut ao, c
             }
             __syncthreads();
         }
+        if (sum) ao.sum.commit(xv, gs.g, gs.cs, gs.h);
     }
 }
 

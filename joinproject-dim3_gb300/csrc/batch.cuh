@@ -437,7 +437,9 @@ static __global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, B
             s_c = Q.rc[s_q];
         }
         __syncthreads();
-        single_bitmap_row(s_c, Q.rs[s_q], s_x, bm, stage);
+        StageSink sink{stage, s_c.out, Q.rs[s_q], s_c.id2x[s_x]};
+        single_bitmap_row(s_c, s_x, bm, sink);
+        sink.flush();
     }
 }
 
@@ -455,7 +457,9 @@ static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, Ba
             s_c = Q.rc[s_q];
         }
         __syncthreads();
-        single_block_row(s_c, Q.rs[s_q], s_x, smem, stage, block_lg);
+        StageSink sink{stage, s_c.out, Q.rs[s_q], s_c.id2x[s_x]};
+        single_block_row(s_c, s_x, smem, sink, block_lg);
+        sink.flush();
     }
 }
 

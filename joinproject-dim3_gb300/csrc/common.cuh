@@ -30,6 +30,49 @@ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     return h;
 }
 
+// Order-independent hashes of output pairs and groups (summaries): the
+// splitmix64 finaliser of x << 32 | z, and of that plus the group's count.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long v) {
+    v = (v ^ (v >> 30)) * 0xbf58476d1ce4e5b9ull;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebull;
+    return v ^ (v >> 31);
+}
+__device__ __forceinline__ unsigned long long pair_hash(uint32_t x, uint32_t z) {
+    return mix64(((unsigned long long)x << 32) | z);
+}
+__device__ __forceinline__ unsigned long long group_hash(uint32_t x, uint32_t z, unsigned long long count) {
+    return mix64(pair_hash(x, z) + count);
+}
+
+// Per-A-tile summary accumulators: tile(a) = mix32(a) & mask; three words a
+// tile (groups, count sum, hash sum).  Rows whose tile is outside [lo, hi)
+// are skipped.
+struct SumAcc {
+    unsigned long long* tiles;  // nullptr: no summary (outputs are written)
+    uint32_t mask, lo, hi;
+    __device__ __forceinline__ uint32_t tile(uint32_t a) const { return mix32(a) & mask; }
+    __device__ __forceinline__ bool selected(uint32_t a) const {
+        const uint32_t t = tile(a);
+        return t >= lo && t < hi;
+    }
+    // warp-collective: adds the lanes' partial sums to a's tile
+    __device__ __forceinline__ void commit(uint32_t a, unsigned long long groups, unsigned long long count_sum,
+                                           unsigned long long hash) const {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            groups += __shfl_xor_sync(0xffffffffu, groups, o);
+            count_sum += __shfl_xor_sync(0xffffffffu, count_sum, o);
+            hash += __shfl_xor_sync(0xffffffffu, hash, o);
+        }
+        if ((threadIdx.x & 31) == 0 && groups) {
+            unsigned long long* t = tiles + 3ull * tile(a);
+            atomicAdd(&t[0], groups);
+            atomicAdd(&t[1], count_sum);
+            atomicAdd(&t[2], hash);
+        }
+    }
+};
+
 // L2 residency: the CSR rows are re-read by many x rows and should stay in
 // L2, while the output pairs stream through once.  Loads of CSR data carry
 // an evict_last policy; output stores use the evict-first (.cs) path.

@@ -109,6 +109,8 @@ struct dim3g_ctx {
     size_t d_in_bytes = 0;
     void* d_out = nullptr;
     size_t d_out_bytes = 0;
+    void* d_sum = nullptr;  // per-A-tile summary accumulators
+    size_t d_sum_bytes = 0;
     Scalars* h_sc = nullptr;  // pinned
     cudaEvent_t ev[6] = {};
     cudaEvent_t evc[8] = {};  // per row-class kernel timing
@@ -201,6 +203,7 @@ struct JoinPlan {
     bool count_only;  // stop after the count pass
     bool single_pass; // one expansion, rows reserve their output range
     OutPrep prep;
+    SumAcc sum{nullptr, 0, 0, 0};  // tiles set: per-A-tile summaries, no output
 };
 
 bool set_aggregate_attributes();
@@ -354,7 +357,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     const uint32_t cap_b = 1u << (c->prm.block_lg - 1);
     // tiny rows get their own warp launch in the single pass only
     const bool tiny = jp.single_pass && !jp.aggregate && !jp.count_only;
-    k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, tiny, ucap, cls,
+    k_row_work<<<grid_for((uint64_t)n * 32, sm), 256, 0, st>>>(rc, n, cap_w, cap_b, jp.aggregate, tiny, jp.sum, ucap, cls,
                                                                 &sc->outj, sc->outj_cls);
     CHECK_LAUNCH();
     uint32_t* list_w = lists;
@@ -384,6 +387,43 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     const unsigned g_b = resident_grid(k_rows_block<true>, blk_b, smem_b, sm);
     const unsigned g_m = resident_grid(k_rows_bitmap<true>, blk_m, smem_m, sm);
 
+    if (jp.sum.tiles) {
+        // summaries: the expansion kernels hash instead of writing; COUNT
+        // needs no count pass (nothing is placed)
+        CU(cudaEventRecord(c->evc[4], st));
+        if (jp.aggregate) {
+            int r = run_aggregate_write(c, rc, AggOut{nullptr, jp.sum}, L);
+            if (r) return r;
+        } else {
+            k_sum_bitmap<<<resident_grid(k_sum_bitmap, blk_m, smem_m, sm), blk_m, smem_m, st>>>(rc, jp.sum, L.m,
+                                                                                            L.n3, L.n4);
+            CHECK_LAUNCH();
+            k_sum_block<<<resident_grid(k_sum_block, blk_b, smem_b, sm), blk_b, smem_b, st>>>(rc, jp.sum, L.b, L.nb,
+                                                                                          c->prm.block_lg);
+            CHECK_LAUNCH();
+            const size_t sw = (size_t)wpc << c->prm.warp_lg << 2;
+            k_sum_warp<<<resident_grid(k_sum_warp, 32 * wpc, sw, sm), 32 * wpc, sw, st>>>(rc, jp.sum, L.w, L.nw,
+                                                                                      c->prm.warp_lg);
+            CHECK_LAUNCH();
+        }
+        CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CU(cudaEventRecord(c->ev[3], st));
+        CU(cudaStreamSynchronize(st));
+        if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in summary (flags %u)", c->h_sc->err);
+        S.out_j = c->h_sc->outj;
+        S.rows_warp = (uint32_t)c->h_sc->nrows[1];
+        S.rows_block = (uint32_t)c->h_sc->nrows[2];
+        S.rows_bitmap = (uint32_t)(c->h_sc->nrows[3] + c->h_sc->nrows[4]);
+        float a, b, e;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&e, c->ev[2], c->ev[3]);
+        S.ms_map = a;
+        S.ms_csr = b;
+        S.ms_write = e;
+        S.ms_total = a + b + e;
+        return DIM3G_OK;
+    }
     if (jp.single_pass && !jp.aggregate && !jp.count_only) {
         uint2* out = nullptr;
         uint64_t cap = 0;
@@ -549,6 +589,9 @@ int run_aggregate_write(dim3g_ctx* c, const RowCtx& rc, AggOut ao, const RowList
 
 bool set_aggregate_attributes() {
     return cudaFuncSetAttribute(k_agg_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess &&
+           cudaFuncSetAttribute(k_sum_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess &&
+           cudaFuncSetAttribute(k_sum_block, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 14 << 2) == cudaSuccess &&
+           cudaFuncSetAttribute(k_sum_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (1 << 20) / 8) == cudaSuccess &&
            cudaFuncSetAttribute(k_agg_block, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 << 14 << 2) == cudaSuccess &&
            cudaFuncSetAttribute(k_agg_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (1 << kAggTileLg) * 4) == cudaSuccess;
 }
@@ -751,6 +794,7 @@ void dim3g_destroy(dim3g_ctx* c) {
     c->ws.release();
     if (c->d_in) cudaFree(c->d_in);
     if (c->d_out) cudaFree(c->d_out);
+    if (c->d_sum) cudaFree(c->d_sum);
     if (c->h_sc) cudaFreeHost(c->h_sc);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -822,8 +866,9 @@ int dim3g_trim(dim3g_ctx* c) {
     c->ws.release();
     if (c->d_in) cudaFree(c->d_in);
     if (c->d_out) cudaFree(c->d_out);
-    c->d_in = c->d_out = nullptr;
-    c->d_in_bytes = c->d_out_bytes = 0;
+    if (c->d_sum) cudaFree(c->d_sum);
+    c->d_in = c->d_out = c->d_sum = nullptr;
+    c->d_in_bytes = c->d_out_bytes = c->d_sum_bytes = 0;
     return DIM3G_OK;
 }
 
@@ -882,6 +927,51 @@ int dim3g_join_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
                 swap, true, false, false, OutPrep{prep_device, peek_device, &d}};
     return run_join(c, jp, n_out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int run_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS, bool aggregate,
+                uint32_t tiles, uint32_t lo, uint32_t hi, dim3g_tile_summary* out) {
+    if (!c || !out || (nR && !dR) || (nS && !dS)) return fail(c, DIM3G_ERR_INVALID, "null argument");
+    if (tiles == 0 || tiles > (1u << 20) || (tiles & (tiles - 1)) || lo >= hi || hi > tiles)
+        return fail(c, DIM3G_ERR_INVALID, "tiles must be a power of two <= 2^20 and lo < hi <= tiles");
+    if (!aligned8(dR) || !aligned8(dS)) return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
+    CU(cudaSetDevice(c->device));
+    memset(out, 0, (size_t)tiles * sizeof(dim3g_tile_summary));
+    // the accumulators live outside the per-call workspace (reset by run_join)
+    int r = ensure_dev(c, &c->d_sum, &c->d_sum_bytes, (size_t)tiles * 24);
+    if (r) return r;
+    CU(cudaMemsetAsync(c->d_sum, 0, (size_t)tiles * 24, c->stream));
+    const bool swap = nR < nS;
+    JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
+                swap, aggregate, false, false, OutPrep{nullptr, nullptr, nullptr}};
+    jp.sum = SumAcc{(unsigned long long*)c->d_sum, tiles - 1, lo, hi};
+    uint64_t n = 0;
+    r = run_join(c, jp, &n);
+    if (r) return r;
+    CU(cudaMemcpyAsync(out, c->d_sum, (size_t)tiles * 24, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    uint64_t groups = 0;
+    for (uint32_t t = 0; t < tiles; t++) groups += out[t].groups;
+    c->stats.n_out = groups;
+    return DIM3G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dim3g_join_project_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
+                               uint32_t tiles, uint32_t tile_lo, uint32_t tile_hi, dim3g_tile_summary* out) {
+    return run_summary(c, dR, nR, dS, nS, false, tiles, tile_lo, tile_hi, out);
+}
+
+int dim3g_join_count_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
+                             uint32_t tiles, uint32_t tile_lo, uint32_t tile_hi, dim3g_tile_summary* out) {
+    return run_summary(c, dR, nR, dS, nS, true, tiles, tile_lo, tile_hi, out);
 }
 
 }  // extern "C"

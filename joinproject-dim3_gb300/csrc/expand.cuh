@@ -431,10 +431,10 @@ static __global__ void __launch_bounds__(1024) k_rows_bitmap(RowCtx c, const uin
 }
 
 // Per-row candidate count w = sum over y in R_x of |S_y|, u = min(w, m) and
-// the row class (0: empty).  One warp per row.  With check_range set
+// the row class (0: empty, or outside sel's A-tiles).  One warp per row.  With check_range set
 // (join-aggregate, 32-bit per-group counters) a row of 2^32 or more
 // candidates raises kErrCountRange.
-static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range, bool tiny,
+static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t cap_b, bool check_range, bool tiny, SumAcc sel,
                            uint32_t* __restrict__ ucap, uint8_t* __restrict__ cls, unsigned long long* outj,
                            unsigned long long* outj_cls) {
     const uint32_t lane = lane_id();
@@ -442,6 +442,13 @@ static __global__ void k_row_work(RowCtx c, uint32_t n, uint32_t cap_w, uint32_t
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long acc = 0, acc_cls[6] = {0, 0, 0, 0, 0, 0};
     for (uint64_t x = gw; x < n; x += nwarps) {
+        if (sel.tiles && !sel.selected(c.id2x[x])) {  // summaries over a slice of A-tiles
+            if (lane == 0) {
+                ucap[x] = 0;
+                cls[x] = 0;
+            }
+            continue;
+        }
         uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
         unsigned long long w = 0;
         for (uint32_t e = e0 + lane; e < e1; e += 32) {

@@ -105,13 +105,35 @@ struct PairStageSink {
     }
 };
 
+// Summary sink: no pairs written; each lane sums pair hashes and counts of
+// its first insertions, committed to the row's A-tile at the end of the row.
+struct HashSink {
+    static constexpr bool kValues = true;
+    uint32_t xv = 0;
+    unsigned long long h = 0, n = 0;
+    template <uint32_t N>
+    __device__ __forceinline__ void take(const uint32_t (&b)[N], const uint32_t (&v)[N]) {
+#pragma unroll
+        for (uint32_t u = 0; u < N; u++)
+            if (b[u] & (1u << lane_id())) {
+                h += pair_hash(xv, v[u]);
+                n++;
+            }
+    }
+    __device__ __forceinline__ void commit(const SumAcc& acc) {
+        acc.commit(xv, n, n, h);
+        h = n = 0;
+    }
+};
+
 // ---- row bodies (shared by the one-join kernels below and the many-query
 // kernels of batch.cuh)
 
 // Class 1: the calling warp expands row x with its own 2^warp_lg-word table
 // (hash set, or a whole-domain bitmap when use_row_bitmap) into the warp's
 // pair sink, which stays open across the warp's rows.
-__device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uint32_t* tab, PairStageSink& sink,
+template <class Sink>
+__device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uint32_t* tab, Sink& sink,
                                                 uint32_t warp_lg) {
     const uint32_t lane = lane_id();
     const uint32_t u = c.ucap[x];
@@ -134,10 +156,12 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uin
 }
 
 // Class 2: the whole CTA expands row x; a 2^block_lg-word table (hash set or
-// whole-domain bitmap) at smem, one staging buffer per warp.  Called by all
-// threads after a barrier that follows the previous row.
-__device__ __forceinline__ void single_block_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* smem,
-                                                 uint32_t* stage, uint32_t block_lg) {
+// whole-domain bitmap) at smem, into each warp's sink (the caller sets its
+// x value and flushes it).  Called by all threads after a barrier that
+// follows the previous row.
+template <class Sink>
+__device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, uint32_t* smem, Sink& sink,
+                                                 uint32_t block_lg) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
     const uint32_t u = c.ucap[x];
@@ -149,7 +173,6 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, const Reserve&
     uint4* t4 = reinterpret_cast<uint4*>(smem);
     for (uint32_t s = threadIdx.x; s < n4; s += blockDim.x) t4[s] = make_uint4(fill, fill, fill, fill);
     __syncthreads();
-    StageSink sink{stage, c.out, rs, c.id2x[x]};
     if (bm) {
         TileBitmap set{smem, 0};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
@@ -157,17 +180,15 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, const Reserve&
         HashSet set{smem, lg, c.err};
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
     }
-    sink.flush();
 }
 
 // Classes 3/4: the whole CTA expands row x one z tile at a time into a
-// bitmap at bm (words rounded up to uint4, at least 32); the warps' staging
-// survives the tiles of the row.
-__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, const Reserve& rs, uint32_t x, uint32_t* bm,
-                                                  uint32_t* stage) {
+// bitmap at bm (words rounded up to uint4, at least 32), into each warp's
+// sink (the caller sets its x value and flushes it once for the row).
+template <class Sink>
+__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, uint32_t* bm, Sink& sink) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    StageSink sink{stage, c.out, rs, c.id2x[x]};
     for (uint32_t t = 0; t < c.T; t++) {
         const uint32_t lo = t * c.tile_width;
         const uint32_t width = min(c.tile_width, c.m - lo);
@@ -179,7 +200,6 @@ __device__ __forceinline__ void single_bitmap_row(const RowCtx& c, const Reserve
         warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
         __syncthreads();
     }
-    sink.flush();
 }
 
 // ---- one join
@@ -213,8 +233,12 @@ static __global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve 
     __shared__ uint32_t s_row;
     uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*nrows_p;
-    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row))
-        single_block_row(c, rs, rows[ri], smem, stage, block_lg);
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
+        const uint32_t x = rows[ri];
+        StageSink sink{stage, c.out, rs, c.id2x[x]};
+        single_block_row(c, x, smem, sink, block_lg);
+        sink.flush();
+    }
 }
 
 // Classes 3/4: one CTA per row; a bitmap of bitmap_words, then one staging
@@ -227,8 +251,58 @@ static __global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve
     __shared__ uint32_t s_row;
     uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
-    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row))
-        single_bitmap_row(c, rs, rows[ri], bm, stage);
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
+        const uint32_t x = rows[ri];
+        StageSink sink{stage, c.out, rs, c.id2x[x]};
+        single_bitmap_row(c, x, bm, sink);
+        sink.flush();
+    }
+}
+
+// ---- summaries (no pairs written): the same row bodies into hash sinks
+
+static __global__ void __launch_bounds__(256) k_sum_warp(RowCtx c, SumAcc acc, const uint32_t* __restrict__ rows,
+                                                         const unsigned long long* __restrict__ nrows_p,
+                                                         uint32_t warp_lg) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t nw = blockDim.x >> 5, wib = threadIdx.x >> 5;
+    uint32_t* tab = smem + ((size_t)wib << warp_lg);
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    HashSink sink;
+    for (uint32_t ri = blockIdx.x * nw + wib; ri < nrows; ri += gridDim.x * nw) {
+        single_warp_row(c, rows[ri], tab, sink, warp_lg);
+        sink.commit(acc);
+    }
+}
+
+static __global__ void __launch_bounds__(1024) k_sum_block(RowCtx c, SumAcc acc, const uint32_t* __restrict__ rows,
+                                                           const unsigned long long* __restrict__ nrows_p,
+                                                           uint32_t block_lg) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_row;
+    const uint32_t nrows = (uint32_t)*nrows_p;
+    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
+        const uint32_t x = rows[ri];
+        HashSink sink;
+        sink.xv = c.id2x[x];
+        single_block_row(c, x, smem, sink, block_lg);
+        sink.commit(acc);
+    }
+}
+
+static __global__ void __launch_bounds__(1024) k_sum_bitmap(RowCtx c, SumAcc acc, const uint32_t* __restrict__ rows,
+                                                            const unsigned long long* __restrict__ n3,
+                                                            const unsigned long long* __restrict__ n4) {
+    extern __shared__ uint32_t bm[];
+    __shared__ uint32_t s_row;
+    const uint32_t nrows = (uint32_t)(*n3 + *n4);
+    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
+        const uint32_t x = rows[ri];
+        HashSink sink;
+        sink.xv = c.id2x[x];
+        single_bitmap_row(c, x, bm, sink);
+        sink.commit(acc);
+    }
 }
 
 }  // namespace dim3g

@@ -73,7 +73,18 @@ EXPORTS = [
     "dim3g_batch_create", "dim3g_batch_run", "dim3g_batch_info", "dim3g_batch_destroy",
     "dim3g_relset_pair_outj", "dim3g_server_create", "dim3g_server_submit", "dim3g_server_wait",
     "dim3g_server_release", "dim3g_server_stats", "dim3g_server_destroy",
+    "dim3g_autotune", "dim3g_tuning_apply", "dim3g_tuning_key", "dim3g_tuning_save", "dim3g_tuning_load",
+    "dim3g_join_project_summary", "dim3g_join_count_summary",
 ]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile_bits_log2", ctypes.c_int32), ("block_threads", ctypes.c_int32),
+                ("block_slots_log2", ctypes.c_int32), ("warp_slots_log2", ctypes.c_int32),
+                ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Result(ctypes.Structure):
@@ -162,6 +173,15 @@ def load(path=LIB_PATH):
     L.dim3g_server_stats.argtypes = [vp, _u64p, _u64p, _u64p, _u64p]
     L.dim3g_server_destroy.argtypes = [vp]
     L.dim3g_server_destroy.restype = None
+    tp = ctypes.POINTER(Tuning)
+    L.dim3g_autotune.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint32, tp]
+    L.dim3g_tuning_apply.argtypes = [vp, tp]
+    L.dim3g_tuning_key.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_uint64]
+    L.dim3g_tuning_save.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
+    L.dim3g_tuning_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
+    for f in (L.dim3g_join_project_summary, L.dim3g_join_count_summary):
+        f.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                      _u64p]
     _lib = L
     return L
 
@@ -262,6 +282,37 @@ class Context:
         return n.value
 
     # ------------------------------------------------------ join-aggregate
+    def _summary(self, fn, dR, nR, dS, nS, tiles, lo, hi):
+        hi = tiles if hi is None else hi
+        out = np.zeros((tiles, 3), dtype=np.uint64)
+        self._check(fn(self.h, _ptr(dR), nR, _ptr(dS), nS, tiles, lo, hi, out.ctypes.data_as(_u64p)))
+        return out
+
+    def join_project_summary(self, dR, nR, dS, nS, tiles=1, lo=0, hi=None):
+        """Per-A-tile (groups, groups, hash) of the join-project, nothing
+        written (see dim3g_join_project_summary): a (tiles, 3) uint64 array."""
+        return self._summary(self.L.dim3g_join_project_summary, dR, nR, dS, nS, tiles, lo, hi)
+
+    def join_count_summary(self, dR, nR, dS, nS, tiles=1, lo=0, hi=None):
+        """Per-A-tile (groups, count sum, hash) of COUNT(*) GROUP BY (a, c)."""
+        return self._summary(self.L.dim3g_join_count_summary, dR, nR, dS, nS, tiles, lo, hi)
+
+    def autotune(self, dR, nR, dS, nS, max_trials=0):
+        """Time the join under candidate knob settings on this input and
+        apply the fastest (see dim3g_autotune); returns the tuning."""
+        t = Tuning()
+        self._check(self.L.dim3g_autotune(self.h, _ptr(dR), nR, _ptr(dS), nS, max_trials, ctypes.byref(t)))
+        return t.as_dict()
+
+    def apply_tuning(self, t):
+        tt = Tuning(**{k: t[k] for k, _ in Tuning._fields_})
+        self._check(self.L.dim3g_tuning_apply(self.h, ctypes.byref(tt)))
+
+    def tuning_key(self, dR, nR, dS, nS):
+        buf = ctypes.create_string_buffer(64)
+        self._check(self.L.dim3g_tuning_key(self.h, _ptr(dR), nR, _ptr(dS), nS, buf, 64))
+        return buf.value.decode()
+
     def join_count(self, R, S):
         """COUNT(*) GROUP BY (x, z): returns ((n, 2) uint32 pairs, (n,) uint64 counts)."""
         R, rp, nr = _pairs(R)
@@ -455,6 +506,22 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def tuning_save(path, key, t):
+    """Append a tuning (dict of Tuning fields) to the cache file."""
+    tt = Tuning(**{k: t[k] for k, _ in Tuning._fields_})
+    rc = load().dim3g_tuning_save(path.encode(), key.encode(), ctypes.byref(tt))
+    if rc != OK:
+        raise Dim3GError(rc, "tuning cache write failed: " + path)
+
+
+def tuning_load(path, key):
+    """The cached tuning of key, or None."""
+    tt = Tuning()
+    if load().dim3g_tuning_load(path.encode(), key.encode(), ctypes.byref(tt)) != OK:
+        return None
+    return tt.as_dict()
 
 
 class Mapper:

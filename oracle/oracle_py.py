@@ -253,6 +253,55 @@ def group_hash(pairs, counts):
         return int(np.sum(g, dtype=np.uint64))
 
 
+def fmix32(v):
+    """murmur3 fmix32 (the A-tile function of the summaries)."""
+    v = np.asarray(v, dtype=np.uint32).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        v ^= v >> np.uint64(16)
+        v = (v * np.uint64(0x85ebca6b)) & np.uint64(0xFFFFFFFF)
+        v ^= v >> np.uint64(13)
+        v = (v * np.uint64(0xc2b2ae35)) & np.uint64(0xFFFFFFFF)
+        v ^= v >> np.uint64(16)
+    return v
+
+
+def tile_summary(pairs, counts, tiles, lo=0, hi=None):
+    """Per-A-tile (groups, count sum, hash) of a result, tile = fmix32(first
+    value) & (tiles - 1): the definition dim3g_join_*_summary computes, for
+    tiles [lo, hi) (others zero).  counts None: join-project (count sum =
+    groups, hash = pair hash)."""
+    hi = tiles if hi is None else hi
+    p = np.asarray(pairs, dtype=np.uint32).reshape(-1, 2)
+    out = np.zeros((tiles, 3), dtype=np.uint64)
+    step = 1 << 24
+    with np.errstate(over="ignore"):
+        for i0 in range(0, p.shape[0], step):  # bounded temporaries
+            q = p[i0:i0 + step]
+            t = (fmix32(q[:, 0]) & np.uint64(tiles - 1)).astype(np.int64)
+            if counts is None:
+                h = mix64(pair_keys(q))
+                c = np.ones(q.shape[0], dtype=np.uint64)
+            else:
+                c = np.asarray(counts[i0:i0 + step], dtype=np.uint64)
+                h = mix64(mix64(pair_keys(q)) + c)
+            if hi - lo == tiles and tiles > 1:
+                order = np.argsort(t, kind="stable")
+                ts, cs, hs = t[order], c[order], h[order]
+                bounds = np.searchsorted(ts, np.arange(tiles + 1))
+                for k in range(tiles):
+                    a, b = bounds[k], bounds[k + 1]
+                    out[k, 0] += np.uint64(b - a)
+                    out[k, 1] += np.sum(cs[a:b], dtype=np.uint64)
+                    out[k, 2] += np.sum(hs[a:b], dtype=np.uint64)
+            else:
+                for k in range(lo, hi):
+                    sel = t == k
+                    out[k, 0] += np.uint64(np.count_nonzero(sel))
+                    out[k, 1] += np.sum(c[sel], dtype=np.uint64)
+                    out[k, 2] += np.sum(h[sel], dtype=np.uint64)
+    return out
+
+
 def sorted_pairs(pairs):
     k = np.sort(pair_keys(pairs))
     return k

@@ -35,3 +35,23 @@ def test_create_without_gpu_fails_cleanly(built):
     import dim3gpu
     with pytest.raises(dim3gpu.Dim3GError):
         dim3gpu.Context(0)
+
+
+def test_tuning_cache_roundtrip(built, tmp_path):
+    """The autotuner's cache is host-only: save / load by key, last line of
+    a key wins, absent keys and files report no entry."""
+    import dim3gpu
+    path = str(tmp_path / "tuning.txt")
+    assert dim3gpu.tuning_load(path, "p24_z20_w3") is None
+    a = {"tile_bits_log2": 18, "block_threads": 256, "block_slots_log2": 13, "warp_slots_log2": 10,
+         "ms": 12.5, "ms_default": 14.0, "trials": 9}
+    b = dict(a, tile_bits_log2=19, ms=11.0)
+    dim3gpu.tuning_save(path, "p24_z20_w3", a)
+    dim3gpu.tuning_save(path, "p20_z16_w5", dict(a, warp_slots_log2=9))
+    dim3gpu.tuning_save(path, "p24_z20_w3", b)
+    got = dim3gpu.tuning_load(path, "p24_z20_w3")
+    assert got["tile_bits_log2"] == 19 and abs(got["ms"] - 11.0) < 1e-3 and got["trials"] == 9
+    assert dim3gpu.tuning_load(path, "p20_z16_w5")["warp_slots_log2"] == 9
+    assert dim3gpu.tuning_load(path, "nope") is None
+    with pytest.raises(dim3gpu.Dim3GError):
+        dim3gpu.tuning_save(path, "has space", a)

@@ -169,3 +169,60 @@ def test_mapper_matches_sequential_insert_semantics(ctx):
     m.clear()
     assert m.insert(np.array([9], dtype=np.uint32)).tolist() == [0]
     m.close()
+
+
+def test_autotune_applies_settings_and_keeps_results_exact(built, golden, tmp_path):
+    """The autotuner times the join under candidate settings, applies the
+    fastest (never slower than the starting settings) and the results under
+    them stay exact; the cache round-trips the chosen settings."""
+    import torch
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    name = "chung_lu_s005"
+    R, S = case_inputs(name, index, arrays)
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    key = c.tuning_key(dR, R.shape[0], dS, S.shape[0])
+    assert key.startswith("p")
+    t = c.autotune(dR, R.shape[0], dS, S.shape[0], max_trials=8)
+    assert 1 <= t["trials"] <= 8 and t["ms"] <= t["ms_default"]
+    for k in ["tile_bits_log2", "block_threads", "block_slots_log2", "warp_slots_log2"]:
+        assert c.get_param(k) == t[k]
+    check_pairs(c.join_project(R, S), index[name], arrays, name)
+    path = str(tmp_path / "t.txt")
+    dim3gpu.tuning_save(path, key, t)
+    c2 = dim3gpu.Context(0)
+    c2.apply_tuning(dim3gpu.tuning_load(path, key))
+    assert c2.get_param("tile_bits_log2") == t["tile_bits_log2"]
+    p, cnt = c2.join_count(R, S)
+    check_groups(p, cnt, index[name], arrays, name)
+    c.close()
+    c2.close()
+
+
+@pytest.mark.parametrize("name", ["grd_small", "grd_swap", "heavy_duplicates", "zipf_1m_s001", "chung_lu_s005",
+                                  "empty_S", "extreme_keys"])
+def test_summaries_match_oracle_per_tile(ctx, golden, name):
+    """Per-A-tile summaries (nothing written) of the join-project and the
+    COUNT join-aggregate equal the oracle's, on all tiles and on a slice."""
+    import torch
+    from oracle import oracle_py as O
+    index, arrays = golden
+    R, S = case_inputs(name, index, arrays)
+    dR = torch.from_numpy(R.view(np.int32)).cuda() if R.shape[0] else 0
+    dS = torch.from_numpy(S.view(np.int32)).cuda() if S.shape[0] else 0
+    wp, n, _, _ = O.join_project(R, S)
+    wg, wc, ng, _, _ = O.join_count(R, S)
+    tiles = 64
+    want_p = O.tile_summary(wp.reshape(-1, 2) if n else np.empty((0, 2), np.uint32), None, tiles)
+    want_c = O.tile_summary(wg.reshape(-1, 2) if ng else np.empty((0, 2), np.uint32),
+                            wc if ng else np.empty(0, np.uint64), tiles)
+    got_p = ctx.join_project_summary(dR, R.shape[0], dS, S.shape[0], tiles)
+    got_c = ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles)
+    assert np.array_equal(got_p, want_p), name
+    assert np.array_equal(got_c, want_c), name
+    assert int(got_p[:, 0].sum()) == index[name]["n_out"]
+    lo, hi = 8, 24
+    sl = ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles, lo, hi)
+    assert np.array_equal(sl[lo:hi], want_c[lo:hi]) and not sl[:lo].any() and not sl[hi:].any()
