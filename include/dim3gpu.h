@@ -71,10 +71,10 @@ const char* dim3g_last_error(const dim3g_ctx* ctx);
 int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
 /* Tuning knobs, validated on set: "warp_slots_log2" (5..14, warp-class hash
  * set size), "block_slots_log2" (8..14, block-class hash set size),
- * "tile_bits_log2" (10..20, bitmap-class z tile width), "heavy_min_len"
- * (minimum S row length for the dense bitmap block; 0 disables it),
- * "ordered_output" (0: one expansion per row, rows in unspecified order;
- * 1: count pass + write pass, pairs grouped by first value). */
+ * "tile_bits_log2" (10..20, bitmap-class z tile width), "ordered_output" (0: one expansion per row, rows in unspecified order;
+ * 1: count pass + write pass, pairs grouped by first value),
+ * "block_threads" (256, 512 or 1024: CTA width of the block class),
+ * "host_direct_output" (1: pinned host outputs written directly). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */
@@ -89,8 +89,12 @@ int dim3g_trim(dim3g_ctx* ctx);
  * ownership of the reference's myvector result (malloc/realloc'd data). */
 int dim3g_join_project(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy,
                        uint64_t nS, uint32_t** out_xz, uint64_t* n_out);
-/* Host input, result into the caller's host buffer of `capacity` pairs
- * (pinned memory gives full copy bandwidth). */
+/* Host input, result into the caller's host buffer of `capacity` pairs.  A
+ * pinned (page-locked, mapped) buffer is written by the kernels directly,
+ * overlapping the transfer with the join ("host_direct_output" = 0 turns
+ * this off); a pageable one is filled by a copy after the join.  On
+ * DIM3G_ERR_CAPACITY *n_out holds the pairs needed and the buffer's contents
+ * are unspecified. */
 int dim3g_join_project_into(dim3g_ctx* ctx, const uint32_t* R_xy, uint64_t nR, const uint32_t* S_zy,
                             uint64_t nS, uint32_t* out_xz, uint64_t capacity, uint64_t* n_out);
 /* Device-resident input and output: d_R, d_S, d_out are device pointers

@@ -76,8 +76,8 @@ struct Params {
     uint32_t block_lg = 14;   // 16384 slots per CTA set  -> class 2 up to 8192
     uint32_t block_threads = 512;  // CTA width of the class-2 kernels
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
-    int64_t heavy_min_len = 0;
     bool ordered = false;     // two-pass, rows in x-id order
+    bool host_direct = true;  // pinned host outputs are written by the kernels directly
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -672,6 +672,20 @@ int host_join(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, u
     cudaStream_t st = c->stream;
     if (nP) CU(cudaMemcpyAsync(dP, P, nP * 8, cudaMemcpyHostToDevice, st));
     if (nQ) CU(cudaMemcpyAsync(dQ, Q, nQ * 8, cudaMemcpyHostToDevice, st));
+    // A pinned host output buffer is mapped into the device's address space:
+    // the single pass stores pairs straight into it (over NVLink-C2C on
+    // GB300), overlapping the transfer with the expansion instead of a copy
+    // after it.
+    if (out_into && !aggregate && !c->prm.ordered && c->prm.host_direct) {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, out_into) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+            pa.devicePointer && aligned8(pa.devicePointer)) {
+            DeviceOut d{(uint2*)pa.devicePointer, nullptr, capacity};
+            JoinPlan jd{dP, nP, dQ, nQ, swap, false, false, true, OutPrep{prep_device, peek_device, &d}};
+            return run_join(c, jd, n_out);
+        }
+        cudaGetLastError();
+    }
     StagingOut so{aggregate};
     // single pass once the staging buffer exists; a result larger than it
     // grows the buffer and runs again
@@ -832,9 +846,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "tile_bits_log2")) {
         if (v < 10 || v > 20) return fail(c, DIM3G_ERR_INVALID, "tile_bits_log2 must be in 10..20");
         c->prm.tile_lg = (uint32_t)v;
-    } else if (!strcmp(name, "heavy_min_len")) {
-        if (v < 0) return fail(c, DIM3G_ERR_INVALID, "heavy_min_len must be >= 0");
-        c->prm.heavy_min_len = v;
+    } else if (!strcmp(name, "host_direct_output")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "host_direct_output must be 0 or 1");
+        c->prm.host_direct = v != 0;
     } else if (!strcmp(name, "block_threads")) {
         if (v != 256 && v != 512 && v != 1024) return fail(c, DIM3G_ERR_INVALID, "block_threads must be 256, 512 or 1024");
         c->prm.block_threads = (uint32_t)v;
@@ -852,9 +866,9 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     if (!strcmp(name, "warp_slots_log2")) *v = c->prm.warp_lg;
     else if (!strcmp(name, "block_slots_log2")) *v = c->prm.block_lg;
     else if (!strcmp(name, "tile_bits_log2")) *v = c->prm.tile_lg;
-    else if (!strcmp(name, "heavy_min_len")) *v = c->prm.heavy_min_len;
     else if (!strcmp(name, "ordered_output")) *v = c->prm.ordered ? 1 : 0;
     else if (!strcmp(name, "block_threads")) *v = c->prm.block_threads;
+    else if (!strcmp(name, "host_direct_output")) *v = c->prm.host_direct ? 1 : 0;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

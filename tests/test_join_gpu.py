@@ -226,3 +226,29 @@ def test_summaries_match_oracle_per_tile(ctx, golden, name):
     lo, hi = 8, 24
     sl = ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles, lo, hi)
     assert np.array_equal(sl[lo:hi], want_c[lo:hi]) and not sl[:lo].any() and not sl[hi:].any()
+
+
+@pytest.mark.parametrize("direct", [1, 0])
+def test_into_pinned_host_buffer(built, golden, direct):
+    """dim3g_join_project_into with a pinned (mapped) host buffer: the
+    kernels store into it directly (host_direct_output = 1) or through the
+    staging copy (0); both exact, and a too-small pinned buffer reports the
+    size needed."""
+    import torch
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    c.set_param("host_direct_output", direct)
+    for name in ["grd_small", "grd_swap", "chung_lu_s005", "zipf_1m_s001", "empty_S"]:
+        R, S = case_inputs(name, index, arrays)
+        need = index[name]["n_out"]
+        out = torch.empty((max(need, 1), 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        n = c.join_project_into(R, S, out)
+        assert n == need
+        check_pairs(out[:n], index[name], arrays, name)
+        if need > 1:
+            small = torch.empty((need // 2, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+            with pytest.raises(dim3gpu.Dim3GError) as e:
+                c.join_project_into(R, S, small)
+            assert e.value.code == dim3gpu.ERR_CAPACITY and c.stats()["n_out"] == need
+    c.close()
