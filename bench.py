@@ -308,10 +308,14 @@ def run_batch(args, rank, world, local_rank):
     pairs = [((dev[2 * i], R.shape[0]), (dev[2 * i + 1], S.shape[0])) for i, (R, S) in enumerate(rels)]
     torch.cuda.synchronize()
     sizer = dim3gpu.Batch(ctx, pairs, [{"op": 0, "capacity": 0} for _ in rels])
-    need = [r["n_out"] for r in sizer.run(check=False)]
+    sized = sizer.run(check=False)
+    need = [r["n_out"] for r in sized]
     sizer.close()
     outs = [torch.empty((max(n, 1), 2), dtype=torch.int32, device="cuda") for n in need]
     b = dim3gpu.Batch(ctx, pairs, [{"op": 0, "capacity": n, "out": o} for n, o in zip(need, outs)])
+    # tile shapes and class thresholds from the autotuner, timing the batch
+    # graph itself; the plain drop-in below runs under the same settings
+    tuning = b.autotune(max_trials=args.tune_trials)
     for _ in range(args.warmup):
         b.run()
     launches0 = ctx.stats()["launches"]
@@ -354,6 +358,8 @@ def run_batch(args, rank, world, local_rank):
         "config": {"workload": "batch512", "desc": WORKLOADS["batch512"], "queries": len(rels),
                    "tuples": int(ntup), "n_out": int(total), "out_j": int(outj),
                    "redraws": int(sum(p["redraws"] for p in params)),
+                   "tuning": {k: tuning[k] for k in ["tile_bits_log2", "block_threads", "block_slots_log2",
+                                                     "warp_slots_log2", "cta_round_robin", "trials"]},
                    "l2": "inputs and outputs > L2; no flush"},
         "graph_device_ms": round(sum(dev_ms) / len(dev_ms), 3),
         "plain_dropin": {"value": round(total / (plain / 1e3) / 1e6, 3), "ms_per_step": round(plain, 3),
@@ -569,6 +575,7 @@ def main():
     ap.add_argument("--traffic", type=float, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-queries", type=int, default=512)
+    ap.add_argument("--tune-trials", type=int, default=12)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=10.0)

@@ -74,7 +74,9 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * "tile_bits_log2" (10..20, bitmap-class z tile width), "ordered_output" (0: one expansion per row, rows in unspecified order;
  * 1: count pass + write pass, pairs grouped by first value),
  * "block_threads" (256, 512 or 1024: CTA width of the block class),
- * "host_direct_output" (1: pinned host outputs written directly). */
+ * "host_direct_output" (1: pinned host outputs written directly),
+ * "cta_round_robin" (CTA rows: 1 = warps take whole chunks in turn,
+ * 0 = every chunk split across the warps). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */
@@ -274,11 +276,12 @@ void dim3g_batch_destroy(dim3g_batch* b);
  * to a model, the join is timed on the caller's device-resident input under
  * candidate settings of the knobs that set the row classes' thresholds and
  * tile shapes (tile_bits_log2, block_threads, block_slots_log2,
- * warp_slots_log2), by coordinate descent from the context's current
+ * warp_slots_log2) and the CTA rows' chunk sharing (cta_round_robin), by
+ * coordinate descent from the context's current
  * settings (always a trial), and the fastest are applied to the context.
  * max_trials bounds the joins run (0: no bound). */
 typedef struct {
-    int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2;
+    int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2, cta_round_robin;
     float ms;          /* best measured device ms of one join */
     float ms_default;  /* the starting settings' ms */
     uint32_t trials;   /* settings timed */
@@ -286,6 +289,10 @@ typedef struct {
 int dim3g_autotune(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,
                    uint32_t max_trials, dim3g_tuning* out);
 int dim3g_tuning_apply(dim3g_ctx* ctx, const dim3g_tuning* t);
+/* The same for a batch: the batch's CUDA graph itself is timed (re-captured
+ * per trial) under candidate settings; the fastest stay applied to the
+ * batch's context and captured.  Outputs are rewritten by every trial. */
+int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out);
 /* Shape signature of a workload ("p<lg |P|>_z<lg |z|>_w<lg candidates per
  * row>"), from one count pass; key_len >= 32. */
 int dim3g_tuning_key(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS, char* key,

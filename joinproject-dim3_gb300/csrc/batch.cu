@@ -86,16 +86,17 @@ unsigned elem_grid(uint64_t n, int sm) {
 }
 
 struct Tuning {
-    uint32_t warp_lg, block_lg, block_threads, tile_lg;
+    uint32_t warp_lg, block_lg, block_threads, tile_lg, cta_rr;
 };
 Tuning tuning_of(const dim3g_ctx* ctx) {
-    int64_t w = 11, b = 14, t = 512, tl = 19;
+    int64_t w = 11, b = 14, t = 512, tl = 19, rr = 0;
     dim3g_get_param(ctx, "warp_slots_log2", &w);
     dim3g_get_param(ctx, "block_slots_log2", &b);
     dim3g_get_param(ctx, "block_threads", &t);
     dim3g_get_param(ctx, "tile_bits_log2", &tl);
+    dim3g_get_param(ctx, "cta_round_robin", &rr);
     if (tl > 19) tl = 19;  // the batch bitmap kernel runs 512-thread CTAs
-    return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl};
+    return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl, (uint32_t)rr};
 }
 
 // Warps per CTA of the warp-class kernels (about half an SM's shared memory).
@@ -442,6 +443,7 @@ int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t
     const int sm = I::sm_count(ctx);
     const Tuning tu = tuning_of(ctx);
     const uint32_t nq = qp.nq;
+    Q.cta_rr = tu.cta_rr;
     BCU(cudaMemsetAsync(qp.ncls, 0, 16 * 8, st));
     BCU(cudaMemsetAsync(Q.cls, 0, qp.nrows, st));
     BCU(cudaMemsetAsync(Q.wrow, 0, qp.nrows * 8, st));
@@ -760,6 +762,81 @@ int dim3g_batch_run(dim3g_batch* b, dim3g_query* q) {
         if (r) return r;
     }
     return I::fail(ctx, DIM3G_ERR_DEVICE, "batch: key space did not converge");
+}
+
+// The autotuner for a batch: the batch graph itself is timed under candidate
+// knob settings (re-captured per trial), coordinate descent as in
+// dim3g_autotune; the fastest settings stay applied and captured.
+int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out) {
+    if (!b || !out) return DIM3G_ERR_INVALID;
+    dim3g_ctx* ctx = b->set.ctx;
+    memset(out, 0, sizeof *out);
+    struct K {
+        const char* name;
+        std::vector<int64_t> values;
+    };
+    const std::vector<K> knobs = {{"cta_round_robin", {0, 1}},
+                                  {"block_slots_log2", {14, 13, 12}},
+                                  {"warp_slots_log2", {11, 10, 9, 12}},
+                                  {"block_threads", {512, 256, 1024}},
+                                  {"tile_bits_log2", {19, 18, 17}}};
+    std::vector<int64_t> best(knobs.size());
+    for (size_t i = 0; i < knobs.size(); i++) {
+        const int r = dim3g_get_param(ctx, knobs[i].name, &best[i]);
+        if (r) return r;
+    }
+    std::vector<dim3g_query> q = b->queries;
+    auto time_it = [&](float* ms) -> int {
+        int r = batch_capture(b);
+        float m = 1e30f;
+        for (int k = 0; k < 2 && !r; k++) {
+            r = dim3g_batch_run(b, q.data());
+            if (b->ms_last < m) m = b->ms_last;
+        }
+        *ms = m;
+        return r;
+    };
+    auto apply = [&](const std::vector<int64_t>& v) -> int {
+        for (size_t i = 0; i < knobs.size(); i++) {
+            const int r = dim3g_set_param(ctx, knobs[i].name, v[i]);
+            if (r) return r;
+        }
+        return DIM3G_OK;
+    };
+    float best_ms = 0;
+    int r = time_it(&best_ms);
+    uint32_t trials = 1;
+    const float ms_default = best_ms;
+    for (size_t i = 0; i < knobs.size() && !r; i++) {
+        for (int64_t v : knobs[i].values) {
+            if (v == best[i]) continue;
+            if (max_trials && trials >= max_trials) break;
+            std::vector<int64_t> cand = best;
+            cand[i] = v;
+            if (apply(cand)) continue;
+            float ms = 0;
+            r = time_it(&ms);
+            trials++;
+            if (r) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+    }
+    const int r2 = apply(best);
+    const int r3 = r2 ? r2 : batch_capture(b);
+    if (r) return r;
+    if (r3) return r3;
+    out->cta_round_robin = (int32_t)best[0];
+    out->block_slots_log2 = (int32_t)best[1];
+    out->warp_slots_log2 = (int32_t)best[2];
+    out->block_threads = (int32_t)best[3];
+    out->tile_bits_log2 = (int32_t)best[4];
+    out->ms = best_ms;
+    out->ms_default = ms_default;
+    out->trials = trials;
+    return DIM3G_OK;
 }
 
 int dim3g_batch_info(const dim3g_batch* b, float* ms_last, uint64_t* launches_per_run, uint64_t* device_bytes) {

@@ -292,6 +292,7 @@ struct QueryPools {
     QueryRes* res;    // nq
     const unsigned long long* yt_need;  // the relation set's key-space check
     uint64_t yt_cap;
+    uint32_t cta_rr;  // the context's CTA-row walk (RowCtx::cta_rr)
 };
 
 // False when the relation set's (y, f tile) key space outgrew its pool: its
@@ -364,6 +365,7 @@ static __global__ void k_q_setup(QueryPools Q) {
     c.T = q.T;
     c.tile_width = q.tile_width;
     c.m = (uint32_t)q.nf;
+    c.cta_rr = Q.cta_rr;
     c.ucap = Q.ucap + Q.qrow_off[qi];
     c.cnt = nullptr;
     c.off = nullptr;
@@ -427,6 +429,8 @@ static __global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, B
     extern __shared__ uint32_t bm[];
     __shared__ uint32_t s_row, s_x, s_q;
     __shared__ RowCtx s_c;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*L.n_a + *L.n_b);
     for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
@@ -438,7 +442,7 @@ static __global__ void __launch_bounds__(1024) k_b_single_bitmap(QueryPools Q, B
         }
         __syncthreads();
         StageSink sink{stage, s_c.out, Q.rs[s_q], s_c.id2x[s_x]};
-        single_bitmap_row(s_c, s_x, bm, sink);
+        single_bitmap_row(s_c, s_x, bm, sink, &s_cc);
         sink.flush();
     }
 }
@@ -447,6 +451,8 @@ static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, Ba
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row, s_x, s_q;
     __shared__ RowCtx s_c;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*L.n_a;
     for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
@@ -458,7 +464,7 @@ static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, Ba
         }
         __syncthreads();
         StageSink sink{stage, s_c.out, Q.rs[s_q], s_c.id2x[s_x]};
-        single_block_row(s_c, s_x, smem, sink, block_lg);
+        single_block_row(s_c, s_x, smem, sink, block_lg, &s_cc);
         sink.flush();
     }
 }

@@ -78,6 +78,7 @@ struct Params {
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     bool ordered = false;     // two-pass, rows in x-id order
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
+    uint32_t cta_rr = 0;      // CTA rows: whole chunks round-robin over warps
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -346,6 +347,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     rc.T = T;
     rc.tile_width = tile_width;
     rc.m = m;
+    rc.cta_rr = c->prm.cta_rr;
     rc.ucap = ucap;
     rc.cnt = cnt;
     rc.off = off;
@@ -846,6 +848,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "tile_bits_log2")) {
         if (v < 10 || v > 20) return fail(c, DIM3G_ERR_INVALID, "tile_bits_log2 must be in 10..20");
         c->prm.tile_lg = (uint32_t)v;
+    } else if (!strcmp(name, "cta_round_robin")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "cta_round_robin must be 0 or 1");
+        c->prm.cta_rr = (uint32_t)v;
     } else if (!strcmp(name, "host_direct_output")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "host_direct_output must be 0 or 1");
         c->prm.host_direct = v != 0;
@@ -869,6 +874,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "ordered_output")) *v = c->prm.ordered ? 1 : 0;
     else if (!strcmp(name, "block_threads")) *v = c->prm.block_threads;
     else if (!strcmp(name, "host_direct_output")) *v = c->prm.host_direct ? 1 : 0;
+    else if (!strcmp(name, "cta_round_robin")) *v = c->prm.cta_rr;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

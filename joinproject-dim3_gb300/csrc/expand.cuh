@@ -64,6 +64,7 @@ struct RowCtx {
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
+    uint32_t cta_rr;       // CTA rows: whole chunks round-robin over warps (cta_expand)
     const uint32_t* ucap;  // per row min(candidates, m)
     uint32_t* cnt;         // per row distinct count (count pass output)
     const unsigned long long* off;  // per row output offset (write pass input)
@@ -127,105 +128,188 @@ constexpr uint32_t kFlatAvgMax = DIM3G_FLAT_AVG;
 //                                   v[u] is the lane's z value when the sink
 //                                   asks for values (Sink::kValues), loaded
 //                                   together with the z id to hide latency
+// One 32-entry chunk of R entries: per lane its S segment over tiles
+// [t0, t1) (start, length), the warp's inclusive / exclusive prefixes of the
+// lengths and the chunk's candidate total.
+struct Chunk {
+    uint32_t s0, len, incl, excl, total;
+};
+
+__device__ __forceinline__ Chunk load_chunk(const RowCtx& c, uint32_t eb, uint32_t e1, uint32_t t0, uint32_t t1,
+                                            uint64_t pol) {
+    Chunk ch;
+    const uint32_t e = eb + lane_id();
+    ch.s0 = 0;
+    ch.len = 0;
+    if (e < e1) {
+        const uint32_t y = ld_keep(&c.IC_R[e], pol);
+        const uint64_t r = (uint64_t)y * c.T;
+        ch.s0 = ld_keep(&c.JR_S[r + t0], pol);
+        ch.len = ld_keep(&c.JR_S[r + t1], pol) - ch.s0;
+    }
+    ch.incl = warp_incl_scan(ch.len);
+    if (__any_sync(0xffffffffu, ch.incl < ch.len)) raise_error(c.err, kErrCountRange);
+    ch.total = __shfl_sync(0xffffffffu, ch.incl, 31);
+    ch.excl = ch.incl - ch.len;
+    return ch;
+}
+
+// Candidates [p0, p1) of a chunk through the set into the sink (the calling
+// warp).  Many short segments: gather across segment boundaries -- each lane
+// finds the segment of its candidate (the number of lanes with incl <= c;
+// incl is nondecreasing over lanes) by a 5-step binary search over the
+// lanes' prefixes, so one group of kUnroll x 32 loads covers many segments
+// with a single memory latency.  Long segments: the lanes stride each
+// segment overlapping the piece, kUnroll x 32 candidates at a time, all
+// loads of a group issued first.
+template <class Set, class Sink>
+__device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, uint32_t p0, uint32_t p1, Set& set,
+                                             Sink& sink, uint64_t pol) {
+    const uint32_t lane = lane_id();
+    const uint32_t nseg = __popc(__ballot_sync(0xffffffffu, ch.len != 0));
+    if (ch.total < kFlatAvgMax * nseg) {
+        for (uint32_t cb = p0; cb < p1; cb += 32 * kUnroll) {
+            uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++) {
+                const uint32_t cc = cb + u * 32 + lane;
+                const bool act = cc < p1;
+                const uint32_t ci = act ? cc : p0;  // idle lanes search a valid index
+                uint32_t k = 0;
+#pragma unroll
+                for (uint32_t step = 16; step >= 1; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, ch.incl, k + step - 1) <= ci) k += step;
+                const uint32_t j = __shfl_sync(0xffffffffu, ch.s0, k) + (ci - __shfl_sync(0xffffffffu, ch.excl, k));
+                z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
+                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
+            }
+            uint32_t b[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++)
+                b[u] = (cb + u * 32 < p1) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
+            sink.take(b, v);
+        }
+        return;
+    }
+    // first segment holding candidate p0: lanes with incl <= p0 form a prefix
+    for (uint32_t k = __popc(__ballot_sync(0xffffffffu, ch.incl <= p0)); k < 32; k++) {
+        const uint32_t kex = __shfl_sync(0xffffffffu, ch.excl, k);
+        if (kex >= p1) break;
+        const uint32_t klen = __shfl_sync(0xffffffffu, ch.len, k);
+        const uint32_t ks0 = __shfl_sync(0xffffffffu, ch.s0, k);
+        const uint32_t lo = (p0 > kex ? p0 - kex : 0);
+        const uint32_t hi = (kex + klen < p1 ? klen : p1 - kex);
+        uint32_t jb = lo;
+        // full groups: kUnroll x 32 candidates, all loads issued first
+        for (; jb + 32 * kUnroll <= hi; jb += 32 * kUnroll) {
+            uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++) {
+                const uint32_t j = ks0 + jb + u * 32 + lane;
+                z[u] = ld_keep(&c.IC_S[j], pol);
+                if (Sink::kValues) v[u] = ld_keep(&c.VS[j], pol);
+            }
+            uint32_t b[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], true));
+            sink.take(b, v);
+        }
+        // tail (< kUnroll x 32 left): all its loads issued together, so one
+        // load latency per segment tail; steps past the end are skipped
+        // warp-uniformly
+        if (jb < hi) {
+            uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++) {
+                const uint32_t j = jb + u * 32 + lane;
+                const bool act = j < hi;
+                z[u] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
+                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
+            }
+            uint32_t b[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++)
+                b[u] = (jb + u * 32 < hi) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
+            sink.take(b, v);
+        }
+    }
+}
+
+// Warp-level expansion of the candidates of R entries [e0, e1) over S tiles
+// [t0, t1).  Entries are taken 32 at a time; a warp prefix sum over their S
+// segment lengths flattens the chunk's candidates into [0, total), which is
+// cut into a power-of-two number (<= 2^nparts_lg) of contiguous pieces of at
+// least kMinPiece candidates; the calling warp takes piece `part`.
+//   set.insert(z, active) -> bool   per lane (false when !active)
+//   sink.take(b[], v[])             warp-collective once per group: b[u] is
+//                                   the ballot of first insertions of step u;
+//                                   v[u] is the lane's z value when the sink
+//                                   asks for values (Sink::kValues), loaded
+//                                   together with the z id to hide latency
 template <class Set, class Sink>
 __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t part,
                                             uint32_t nparts_lg, uint32_t t0, uint32_t t1, Set& set, Sink& sink) {
-    const uint32_t lane = lane_id();
     const uint64_t pol = l2_keep_policy();
     for (uint32_t eb = e0; eb < e1; eb += 32) {
-        const uint32_t e = eb + lane;
-        uint32_t s0 = 0, len = 0;
-        if (e < e1) {
-            const uint32_t y = ld_keep(&c.IC_R[e], pol);
-            const uint64_t r = (uint64_t)y * c.T;
-            s0 = ld_keep(&c.JR_S[r + t0], pol);
-            len = ld_keep(&c.JR_S[r + t1], pol) - s0;
-        }
-        const uint32_t incl = warp_incl_scan(len);
-        if (__any_sync(0xffffffffu, incl < len)) raise_error(c.err, kErrCountRange);
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        const uint32_t want = total / kMinPiece;
+        const Chunk ch = load_chunk(c, eb, e1, t0, t1, pol);
+        const uint32_t want = ch.total / kMinPiece;
         uint32_t np_lg = want <= 1 ? 0 : 31 - __clz(want);
         np_lg = np_lg > nparts_lg ? nparts_lg : np_lg;
         if (part >= (1u << np_lg)) continue;
-        const uint32_t piece = (total >> np_lg) + ((total & ((1u << np_lg) - 1)) ? 1u : 0u);
-        const uint32_t p0 = min(part * piece, total);
-        const uint32_t p1 = min(p0 + piece, total);
-        if (p0 >= p1) continue;
-        const uint32_t excl = incl - len;
-        // Many short segments: gather across segment boundaries.  Each lane
-        // finds the segment of its candidate c (the number of lanes with
-        // incl <= c; incl is nondecreasing over lanes) by a 5-step binary
-        // search over the lanes' prefixes, so one group of kUnroll x 32
-        // loads covers many segments with a single memory latency.
-        const uint32_t nseg = __popc(__ballot_sync(0xffffffffu, len != 0));
-        if (total < kFlatAvgMax * nseg) {
-            for (uint32_t cb = p0; cb < p1; cb += 32 * kUnroll) {
-                uint32_t z[kUnroll], v[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++) {
-                    const uint32_t cc = cb + u * 32 + lane;
-                    const bool act = cc < p1;
-                    const uint32_t ci = act ? cc : p0;  // idle lanes search a valid index
-                    uint32_t k = 0;
-#pragma unroll
-                    for (uint32_t step = 16; step >= 1; step >>= 1)
-                        if (__shfl_sync(0xffffffffu, incl, k + step - 1) <= ci) k += step;
-                    const uint32_t j = __shfl_sync(0xffffffffu, s0, k) + (ci - __shfl_sync(0xffffffffu, excl, k));
-                    z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
-                    if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
-                }
-                uint32_t b[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++)
-                    b[u] = (cb + u * 32 < p1) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
-                sink.take(b, v);
-            }
-            continue;
-        }
-        // first segment holding candidate p0: lanes with incl <= p0 form a prefix
-        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, incl <= p0)); k < 32; k++) {
-            const uint32_t kex = __shfl_sync(0xffffffffu, excl, k);
-            if (kex >= p1) break;
-            const uint32_t klen = __shfl_sync(0xffffffffu, len, k);
-            const uint32_t ks0 = __shfl_sync(0xffffffffu, s0, k);
-            const uint32_t lo = (p0 > kex ? p0 - kex : 0);
-            const uint32_t hi = (kex + klen < p1 ? klen : p1 - kex);
-            uint32_t jb = lo;
-            // full groups: kUnroll x 32 candidates, all loads issued first
-            for (; jb + 32 * kUnroll <= hi; jb += 32 * kUnroll) {
-                uint32_t z[kUnroll], v[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++) {
-                    const uint32_t j = ks0 + jb + u * 32 + lane;
-                    z[u] = ld_keep(&c.IC_S[j], pol);
-                    if (Sink::kValues) v[u] = ld_keep(&c.VS[j], pol);
-                }
-                uint32_t b[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], true));
-                sink.take(b, v);
-            }
-            // tail (< kUnroll x 32 left): all its loads issued together, so
-            // one load latency per segment tail; steps past the end are
-            // skipped warp-uniformly
-            if (jb < hi) {
-                uint32_t z[kUnroll], v[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++) {
-                    const uint32_t j = jb + u * 32 + lane;
-                    const bool act = j < hi;
-                    z[u] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
-                    if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
-                }
-                uint32_t b[kUnroll];
-#pragma unroll
-                for (uint32_t u = 0; u < kUnroll; u++)
-                    b[u] = (jb + u * 32 < hi) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
-                sink.take(b, v);
-            }
-        }
+        const uint32_t piece = (ch.total >> np_lg) + ((ch.total & ((1u << np_lg) - 1)) ? 1u : 0u);
+        const uint32_t p0 = min(part * piece, ch.total);
+        const uint32_t p1 = min(p0 + piece, ch.total);
+        if (p0 < p1) expand_piece(c, ch, p0, p1, set, sink, pol);
     }
+}
+
+// Chunks a CTA defers to its cooperative phase (see cta_expand).
+constexpr uint32_t kBigChunk = 4096, kBigCap = 64;
+struct CtaChunks {
+    uint32_t n;              // deferred chunks (may exceed kBigCap: the rest ran at once)
+    uint32_t eb[kBigCap];
+};
+
+// CTA-level expansion of R entries [e0, e1) over S tiles [t0, t1), called
+// by all warps of the CTA (2^nw_lg of them) with the same arguments.  With
+// c.cta_rr set and at least as many chunks as warps, each warp takes whole
+// chunks round-robin -- a chunk's entries and segment bounds are loaded by
+// one warp, not by every warp -- and chunks of more than kBigChunk
+// candidates are deferred and then split across all warps.  Otherwise every
+// chunk is split across the warps (warp_expand).  Which is faster depends on
+// the workload (the autotuner times both).  cc->n must be 0
+// on entry (it is 0 again on return); contains barriers.
+template <class Set, class Sink>
+__device__ __forceinline__ void cta_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t wib, uint32_t nw_lg,
+                                           uint32_t t0, uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
+    const uint32_t nchunks = (e1 - e0 + 31) >> 5;
+    if (!c.cta_rr || nchunks < (1u << nw_lg)) {
+        warp_expand(c, e0, e1, wib, nw_lg, t0, t1, set, sink);
+        return;
+    }
+    const uint64_t pol = l2_keep_policy();
+    for (uint32_t ci = wib; ci < nchunks; ci += 1u << nw_lg) {
+        const uint32_t eb = e0 + 32 * ci;
+        const Chunk ch = load_chunk(c, eb, e1, t0, t1, pol);
+        if (ch.total > kBigChunk) {
+            uint32_t slot = 0;
+            if (lane_id() == 0) slot = atomicAdd(&cc->n, 1u);
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (slot < kBigCap) {
+                if (lane_id() == 0) cc->eb[slot] = eb;
+                continue;
+            }
+        }
+        if (ch.total) expand_piece(c, ch, 0, ch.total, set, sink, pol);
+    }
+    __syncthreads();
+    const uint32_t nbig = min(cc->n, kBigCap);
+    for (uint32_t i = 0; i < nbig; i++) {
+        const uint32_t eb = cc->eb[i];
+        warp_expand(c, eb, min(eb + 32, e1), wib, nw_lg, t0, t1, set, sink);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) cc->n = 0;
 }
 
 // ----------------------------------------------------------------- sets

@@ -161,7 +161,7 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uin
 // follows the previous row.
 template <class Sink>
 __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, uint32_t* smem, Sink& sink,
-                                                 uint32_t block_lg) {
+                                                 uint32_t block_lg, CtaChunks* cc) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
     const uint32_t u = c.ucap[x];
@@ -175,10 +175,10 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
     __syncthreads();
     if (bm) {
         TileBitmap set{smem, 0};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink, cc);
     } else {
         HashSet set{smem, lg, c.err};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink);
+        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink, cc);
     }
 }
 
@@ -186,7 +186,8 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
 // bitmap at bm (words rounded up to uint4, at least 32), into each warp's
 // sink (the caller sets its x value and flushes it once for the row).
 template <class Sink>
-__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, uint32_t* bm, Sink& sink) {
+__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, uint32_t* bm, Sink& sink,
+                                                  CtaChunks* cc) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
     for (uint32_t t = 0; t < c.T; t++) {
@@ -197,7 +198,7 @@ __device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, u
         for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
         __syncthreads();
         TileBitmap set{bm, lo};
-        warp_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink);
+        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink, cc);
         __syncthreads();
     }
 }
@@ -231,12 +232,14 @@ static __global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve 
                                                               uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
         StageSink sink{stage, c.out, rs, c.id2x[x]};
-        single_block_row(c, x, smem, sink, block_lg);
+        single_block_row(c, x, smem, sink, block_lg, &s_cc);
         sink.flush();
     }
 }
@@ -249,12 +252,14 @@ static __global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve
                                                                uint32_t bitmap_words) {
     extern __shared__ uint32_t bm[];
     __shared__ uint32_t s_row;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
     for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
         const uint32_t x = rows[ri];
         StageSink sink{stage, c.out, rs, c.id2x[x]};
-        single_bitmap_row(c, x, bm, sink);
+        single_bitmap_row(c, x, bm, sink, &s_cc);
         sink.flush();
     }
 }
@@ -280,12 +285,14 @@ static __global__ void __launch_bounds__(1024) k_sum_block(RowCtx c, SumAcc acc,
                                                            uint32_t block_lg) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     const uint32_t nrows = (uint32_t)*nrows_p;
     for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
         const uint32_t x = rows[ri];
         HashSink sink;
         sink.xv = c.id2x[x];
-        single_block_row(c, x, smem, sink, block_lg);
+        single_block_row(c, x, smem, sink, block_lg, &s_cc);
         sink.commit(acc);
     }
 }
@@ -295,12 +302,14 @@ static __global__ void __launch_bounds__(1024) k_sum_bitmap(RowCtx c, SumAcc acc
                                                             const unsigned long long* __restrict__ n4) {
     extern __shared__ uint32_t bm[];
     __shared__ uint32_t s_row;
+    __shared__ CtaChunks s_cc;
+    if (threadIdx.x == 0) s_cc.n = 0;
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
     for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
         const uint32_t x = rows[ri];
         HashSink sink;
         sink.xv = c.id2x[x];
-        single_bitmap_row(c, x, bm, sink);
+        single_bitmap_row(c, x, bm, sink, &s_cc);
         sink.commit(acc);
     }
 }

@@ -74,14 +74,14 @@ EXPORTS = [
     "dim3g_relset_pair_outj", "dim3g_server_create", "dim3g_server_submit", "dim3g_server_wait",
     "dim3g_server_release", "dim3g_server_stats", "dim3g_server_destroy",
     "dim3g_autotune", "dim3g_tuning_apply", "dim3g_tuning_key", "dim3g_tuning_save", "dim3g_tuning_load",
-    "dim3g_join_project_summary", "dim3g_join_count_summary",
+    "dim3g_join_project_summary", "dim3g_join_count_summary", "dim3g_batch_autotune",
 ]
 
 
 class Tuning(ctypes.Structure):
     _fields_ = [("tile_bits_log2", ctypes.c_int32), ("block_threads", ctypes.c_int32),
                 ("block_slots_log2", ctypes.c_int32), ("warp_slots_log2", ctypes.c_int32),
-                ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
+                ("cta_round_robin", ctypes.c_int32), ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -179,6 +179,7 @@ def load(path=LIB_PATH):
     L.dim3g_tuning_key.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_uint64]
     L.dim3g_tuning_save.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
     L.dim3g_tuning_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
+    L.dim3g_batch_autotune.argtypes = [vp, ctypes.c_uint32, tp]
     for f in (L.dim3g_join_project_summary, L.dim3g_join_count_summary):
         f.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                       _u64p]
@@ -490,6 +491,13 @@ class Batch:
         if check:
             self.ctx._check(rc)
         return _results(self.q)
+
+    def autotune(self, max_trials=0):
+        """Time the batch graph under candidate knob settings and keep the
+        fastest (see dim3g_batch_autotune)."""
+        t = Tuning()
+        self.ctx._check(self.L.dim3g_batch_autotune(self.h, max_trials, ctypes.byref(t)))
+        return t.as_dict()
 
     def info(self):
         ms, nl, nb = ctypes.c_float(), ctypes.c_uint64(), ctypes.c_uint64()

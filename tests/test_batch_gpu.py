@@ -162,3 +162,21 @@ def test_batch_graph_matches_golden_and_replays(ctx, golden):
     info = b.info()
     assert info["launches_per_run"] > 0 and info["ms_last"] > 0
     b.close()
+
+
+def test_batch_autotune_keeps_results_exact(built, golden):
+    """The batch autotuner re-captures and times the graph under candidate
+    settings; afterwards the graph (with the chosen settings) is exact."""
+    import dim3gpu
+    c = dim3gpu.Context(0)
+    names = ["grd_small", "grd_swap", "zipf_1m_s001", "chung_lu_s005", "heavy_duplicates"]
+    _, rels = _inputs(golden, names)
+    pairs = [(rels[2 * i], rels[2 * i + 1]) for i in range(len(names))]
+    specs = _specs(golden, names, [dim3gpu.OP_PROJECT])
+    b = dim3gpu.Batch(c, pairs, specs)
+    t = b.autotune(max_trials=6)
+    assert 1 <= t["trials"] <= 6 and t["ms"] <= t["ms_default"]
+    assert c.get_param("cta_round_robin") == t["cta_round_robin"]
+    _check(golden, specs, b.run())
+    b.close()
+    c.close()
