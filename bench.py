@@ -359,7 +359,7 @@ def run_batch(args, rank, world, local_rank):
                    "tuples": int(ntup), "n_out": int(total), "out_j": int(outj),
                    "redraws": int(sum(p["redraws"] for p in params)),
                    "tuning": {k: tuning[k] for k in ["tile_bits_log2", "block_threads", "block_slots_log2",
-                                                     "warp_slots_log2", "cta_round_robin", "trials"]},
+                                                     "warp_slots_log2", "cta_walk", "trials"]},
                    "l2": "inputs and outputs > L2; no flush"},
         "graph_device_ms": round(sum(dev_ms) / len(dev_ms), 3),
         "plain_dropin": {"value": round(total / (plain / 1e3) / 1e6, 3), "ms_per_step": round(plain, 3),

@@ -75,8 +75,10 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * 1: count pass + write pass, pairs grouped by first value),
  * "block_threads" (256, 512 or 1024: CTA width of the block class),
  * "host_direct_output" (1: pinned host outputs written directly),
- * "cta_round_robin" (CTA rows: 1 = warps take whole chunks in turn,
- * 0 = every chunk split across the warps). */
+ * "cta_walk" (how CTA rows share candidates among warps: 0 = the row's
+ * segment table staged in shared memory and its candidates split evenly,
+ * 1 = warps take whole 32-entry chunks in turn, 2 = every chunk split
+ * across the warps). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */
@@ -276,12 +278,12 @@ void dim3g_batch_destroy(dim3g_batch* b);
  * to a model, the join is timed on the caller's device-resident input under
  * candidate settings of the knobs that set the row classes' thresholds and
  * tile shapes (tile_bits_log2, block_threads, block_slots_log2,
- * warp_slots_log2) and the CTA rows' chunk sharing (cta_round_robin), by
+ * warp_slots_log2) and the CTA rows' walk (cta_walk), by
  * coordinate descent from the context's current
  * settings (always a trial), and the fastest are applied to the context.
  * max_trials bounds the joins run (0: no bound). */
 typedef struct {
-    int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2, cta_round_robin;
+    int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2, cta_walk;
     float ms;          /* best measured device ms of one join */
     float ms_default;  /* the starting settings' ms */
     uint32_t trials;   /* settings timed */

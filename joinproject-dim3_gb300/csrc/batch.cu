@@ -89,12 +89,12 @@ struct Tuning {
     uint32_t warp_lg, block_lg, block_threads, tile_lg, cta_rr;
 };
 Tuning tuning_of(const dim3g_ctx* ctx) {
-    int64_t w = 11, b = 14, t = 512, tl = 19, rr = 0;
+    int64_t w = 11, b = 14, t = 512, tl = 19, rr = 2;
     dim3g_get_param(ctx, "warp_slots_log2", &w);
     dim3g_get_param(ctx, "block_slots_log2", &b);
     dim3g_get_param(ctx, "block_threads", &t);
     dim3g_get_param(ctx, "tile_bits_log2", &tl);
-    dim3g_get_param(ctx, "cta_round_robin", &rr);
+    dim3g_get_param(ctx, "cta_walk", &rr);
     if (tl > 19) tl = 19;  // the batch bitmap kernel runs 512-thread CTAs
     return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl, (uint32_t)rr};
 }
@@ -775,7 +775,7 @@ int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out)
         const char* name;
         std::vector<int64_t> values;
     };
-    const std::vector<K> knobs = {{"cta_round_robin", {0, 1}},
+    const std::vector<K> knobs = {{"cta_walk", {0, 1, 2}},
                                   {"block_slots_log2", {14, 13, 12}},
                                   {"warp_slots_log2", {11, 10, 9, 12}},
                                   {"block_threads", {512, 256, 1024}},
@@ -828,7 +828,7 @@ int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out)
     const int r3 = r2 ? r2 : batch_capture(b);
     if (r) return r;
     if (r3) return r3;
-    out->cta_round_robin = (int32_t)best[0];
+    out->cta_walk = (int32_t)best[0];
     out->block_slots_log2 = (int32_t)best[1];
     out->warp_slots_log2 = (int32_t)best[2];
     out->block_threads = (int32_t)best[3];

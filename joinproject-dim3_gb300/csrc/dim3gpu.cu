@@ -78,7 +78,7 @@ struct Params {
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     bool ordered = false;     // two-pass, rows in x-id order
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
-    uint32_t cta_rr = 0;      // CTA rows: whole chunks round-robin over warps
+    uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -848,8 +848,8 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "tile_bits_log2")) {
         if (v < 10 || v > 20) return fail(c, DIM3G_ERR_INVALID, "tile_bits_log2 must be in 10..20");
         c->prm.tile_lg = (uint32_t)v;
-    } else if (!strcmp(name, "cta_round_robin")) {
-        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "cta_round_robin must be 0 or 1");
+    } else if (!strcmp(name, "cta_walk")) {
+        if (v < 0 || v > 2) return fail(c, DIM3G_ERR_INVALID, "cta_walk must be 0, 1 or 2");
         c->prm.cta_rr = (uint32_t)v;
     } else if (!strcmp(name, "host_direct_output")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "host_direct_output must be 0 or 1");
@@ -874,7 +874,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "ordered_output")) *v = c->prm.ordered ? 1 : 0;
     else if (!strcmp(name, "block_threads")) *v = c->prm.block_threads;
     else if (!strcmp(name, "host_direct_output")) *v = c->prm.host_direct ? 1 : 0;
-    else if (!strcmp(name, "cta_round_robin")) *v = c->prm.cta_rr;
+    else if (!strcmp(name, "cta_walk")) *v = c->prm.cta_rr;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

@@ -64,7 +64,7 @@ struct RowCtx {
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
-    uint32_t cta_rr;       // CTA rows: whole chunks round-robin over warps (cta_expand)
+    uint32_t cta_rr;       // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split (cta_expand)
     const uint32_t* ucap;  // per row min(candidates, m)
     uint32_t* cnt;         // per row distinct count (count pass output)
     const unsigned long long* off;  // per row output offset (write pass input)
@@ -263,16 +263,107 @@ __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32
     }
 }
 
-// Chunks a CTA defers to its cooperative phase (see cta_expand).
+// Chunks a CTA defers to its cooperative phase (round-robin walk), and the
+// staged segment table of the row-flattened walk (see cta_expand).
 constexpr uint32_t kBigChunk = 4096, kBigCap = 64;
+constexpr uint32_t kRowBlk = 1024;  // R entries staged at a time by the flattened walk
 struct CtaChunks {
     uint32_t n;              // deferred chunks (may exceed kBigCap: the rest ran at once)
     uint32_t eb[kBigCap];
+    uint32_t s0[kRowBlk];    // flattened walk: segment start of each staged entry
+    uint32_t incl[kRowBlk];  // and the inclusive prefix of the segment lengths
 };
 
+// Row-flattened CTA walk over R entries [e0, e1) and S tiles [t0, t1): the
+// CTA stages kRowBlk entries' segment bounds in shared memory at once (one
+// load latency for the whole block instead of one per 32-entry chunk),
+// scans their lengths CTA-wide and splits the block's candidates evenly
+// over the warps; each lane finds its candidate's segment by binary search
+// in the staged prefixes.  Contains barriers; called by the whole CTA.
+template <class Set, class Sink>
+__device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t t0, uint32_t t1,
+                                                Set& set, Sink& sink, CtaChunks* cc) {
+    const uint32_t tid = threadIdx.x, lane = lane_id(), wib = tid >> 5, nw = blockDim.x >> 5;
+    const uint32_t per = (kRowBlk + blockDim.x - 1) / blockDim.x;  // entries per thread (<= 4)
+    const uint64_t pol = l2_keep_policy();
+    __shared__ uint32_t sm_scan[1024 / 32 + 1];
+    for (uint32_t eb = e0; eb < e1; eb += kRowBlk) {
+        const uint32_t ne = min(kRowBlk, e1 - eb);
+        // stage: thread tid owns entries [tid*per, tid*per + per)
+        uint32_t s0[4], len[4], sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++) {
+            s0[k] = 0;
+            len[k] = 0;
+            const uint32_t i = tid * per + k;
+            if (k < per && i < ne) {
+                const uint32_t y = ld_keep(&c.IC_R[eb + i], pol);
+                const uint64_t r = (uint64_t)y * c.T;
+                s0[k] = ld_keep(&c.JR_S[r + t0], pol);
+                len[k] = ld_keep(&c.JR_S[r + t1], pol) - s0[k];
+                sum += len[k];
+            }
+        }
+        // CTA-wide exclusive scan of the threads' sums (blockDim <= 1024)
+        const uint32_t inc = warp_incl_scan(sum);
+        if (lane == 31) sm_scan[wib] = inc;
+        __syncthreads();
+        if (wib == 0) {
+            const uint32_t v = lane < nw ? sm_scan[lane] : 0u;
+            const uint32_t vi = warp_incl_scan(v);
+            if (lane < nw) sm_scan[lane] = vi - v;
+            if (lane == nw - 1) sm_scan[nw] = vi;
+        }
+        __syncthreads();
+        uint32_t run = sm_scan[wib] + inc - sum;
+        if (sm_scan[nw] < run) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++) {
+            const uint32_t i = tid * per + k;
+            if (k < per && i < ne) {
+                run += len[k];
+                cc->s0[i] = s0[k];
+                cc->incl[i] = run;
+            }
+        }
+        const uint32_t total = sm_scan[nw];
+        __syncthreads();
+        // the warps' even shares of the block's candidates
+        const uint32_t piece = (total + nw - 1) / nw;
+        const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
+        for (uint32_t cb = p0; cb < p1; cb += 32 * kUnroll) {
+            uint32_t z[kUnroll], v[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++) {
+                const uint32_t ci = cb + u * 32 + lane;
+                const bool act = ci < p1;
+                // first staged entry with incl > ci
+                uint32_t lo = 0, hi = ne - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (cc->incl[mid] > ci) hi = mid;
+                    else lo = mid + 1;
+                }
+                const uint32_t excl = lo ? cc->incl[lo - 1] : 0u;
+                const uint32_t j = cc->s0[lo] + (ci - excl);
+                z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
+                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
+            }
+            uint32_t b[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; u++)
+                b[u] = (cb + u * 32 < p1) ? __ballot_sync(0xffffffffu, set.insert(z[u], z[u] != kEmpty32)) : 0u;
+            sink.take(b, v);
+        }
+        __syncthreads();  // the staged table is rewritten by the next block
+    }
+}
+
 // CTA-level expansion of R entries [e0, e1) over S tiles [t0, t1), called
-// by all warps of the CTA (2^nw_lg of them) with the same arguments.  With
-// c.cta_rr set and at least as many chunks as warps, each warp takes whole
+// by all warps of the CTA (2^nw_lg of them) with the same arguments.
+// c.cta_rr selects the walk: 0 the row-flattened walk (cta_expand_flat),
+// 2 every chunk split across the warps (warp_expand), 1 with at least as
+// many chunks as warps, each warp takes whole
 // chunks round-robin -- a chunk's entries and segment bounds are loaded by
 // one warp, not by every warp -- and chunks of more than kBigChunk
 // candidates are deferred and then split across all warps.  Otherwise every
@@ -283,7 +374,11 @@ template <class Set, class Sink>
 __device__ __forceinline__ void cta_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t wib, uint32_t nw_lg,
                                            uint32_t t0, uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
     const uint32_t nchunks = (e1 - e0 + 31) >> 5;
-    if (!c.cta_rr || nchunks < (1u << nw_lg)) {
+    if (c.cta_rr == 0) {
+        cta_expand_flat(c, e0, e1, t0, t1, set, sink, cc);
+        return;
+    }
+    if (c.cta_rr == 2 || nchunks < (1u << nw_lg)) {
         warp_expand(c, e0, e1, wib, nw_lg, t0, t1, set, sink);
         return;
     }

@@ -16,7 +16,10 @@
 
 namespace dim3g {
 
-constexpr uint32_t kStage = 512;  // staged z values per warp (2 KB)
+#ifndef DIM3G_STAGE
+#define DIM3G_STAGE 512
+#endif
+constexpr uint32_t kStage = DIM3G_STAGE;  // staged z values per warp (2 KB)
 
 struct Reserve {
     unsigned long long* cursor;

@@ -10,7 +10,7 @@
 //   block_threads     CTA width of the CTA classes
 //   block_slots_log2  CTA hash-set size (the class 2 / class 3 threshold)
 //   warp_slots_log2   warp hash-set size (the class 1 / class 2 threshold)
-//   cta_round_robin   how CTA rows share their chunks among warps
+//   cta_walk          how CTA rows share their candidates among warps
 // by coordinate descent (one knob at a time, the others at their best so
 // far; the starting settings are always a trial), and the fastest settings
 // are applied to the context.  Results can be kept in a text cache keyed by
@@ -95,7 +95,7 @@ int dim3g_autotune(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint3
                                {"block_threads", {512, 256, 1024}},
                                {"block_slots_log2", {14, 13, 12}},
                                {"warp_slots_log2", {11, 10, 9, 12}},
-                               {"cta_round_robin", {0, 1}}};
+                               {"cta_walk", {0, 1, 2}}};
     std::vector<int64_t> cur(knobs.size());
     for (size_t i = 0; i < knobs.size(); i++) {
         const int r = dim3g_get_param(ctx, knobs[i].name, &cur[i]);
@@ -148,7 +148,7 @@ int dim3g_autotune(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint3
     out->block_threads = (int32_t)best[1];
     out->block_slots_log2 = (int32_t)best[2];
     out->warp_slots_log2 = (int32_t)best[3];
-    out->cta_round_robin = (int32_t)best[4];
+    out->cta_walk = (int32_t)best[4];
     out->ms = best_ms;
     out->ms_default = ms_default;
     out->trials = trials;
@@ -161,12 +161,12 @@ int dim3g_tuning_apply(dim3g_ctx* ctx, const dim3g_tuning* t) {
     if (!r) r = dim3g_set_param(ctx, "block_slots_log2", t->block_slots_log2);
     if (!r) r = dim3g_set_param(ctx, "warp_slots_log2", t->warp_slots_log2);
     if (!r) r = dim3g_set_param(ctx, "block_threads", t->block_threads);
-    if (!r) r = dim3g_set_param(ctx, "cta_round_robin", t->cta_round_robin);
+    if (!r) r = dim3g_set_param(ctx, "cta_walk", t->cta_walk);
     return r;
 }
 
 // Cache file: one line per key,
-// "key tile block_threads block_lg warp_lg cta_round_robin ms ms_default trials".
+// "key tile block_threads block_lg warp_lg cta_walk ms ms_default trials".
 int dim3g_tuning_load(const char* path, const char* key, dim3g_tuning* out) {
     if (!path || !key || !out) return DIM3G_ERR_INVALID;
     FILE* f = fopen(path, "r");
@@ -175,7 +175,7 @@ int dim3g_tuning_load(const char* path, const char* key, dim3g_tuning* out) {
     dim3g_tuning t{};
     int found = 0;
     while (fscanf(f, "%127s %d %d %d %d %d %f %f %u", k, &t.tile_bits_log2, &t.block_threads, &t.block_slots_log2,
-                  &t.warp_slots_log2, &t.cta_round_robin, &t.ms, &t.ms_default, &t.trials) == 9) {
+                  &t.warp_slots_log2, &t.cta_walk, &t.ms, &t.ms_default, &t.trials) == 9) {
         if (!strcmp(k, key)) {
             *out = t;
             found = 1;  // the last line for a key wins
@@ -190,7 +190,7 @@ int dim3g_tuning_save(const char* path, const char* key, const dim3g_tuning* t) 
     FILE* f = fopen(path, "a");
     if (!f) return DIM3G_ERR_INVALID;
     const int w = fprintf(f, "%s %d %d %d %d %d %.4f %.4f %u\n", key, t->tile_bits_log2, t->block_threads,
-                          t->block_slots_log2, t->warp_slots_log2, t->cta_round_robin, t->ms, t->ms_default,
+                          t->block_slots_log2, t->warp_slots_log2, t->cta_walk, t->ms, t->ms_default,
                           t->trials);
     fclose(f);
     return w > 0 ? DIM3G_OK : DIM3G_ERR_INVALID;

@@ -81,7 +81,7 @@ EXPORTS = [
 class Tuning(ctypes.Structure):
     _fields_ = [("tile_bits_log2", ctypes.c_int32), ("block_threads", ctypes.c_int32),
                 ("block_slots_log2", ctypes.c_int32), ("warp_slots_log2", ctypes.c_int32),
-                ("cta_round_robin", ctypes.c_int32), ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
+                ("cta_walk", ctypes.c_int32), ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -44,7 +44,7 @@ def test_tuning_cache_roundtrip(built, tmp_path):
     path = str(tmp_path / "tuning.txt")
     assert dim3gpu.tuning_load(path, "p24_z20_w3") is None
     a = {"tile_bits_log2": 18, "block_threads": 256, "block_slots_log2": 13, "warp_slots_log2": 10,
-         "cta_round_robin": 1, "ms": 12.5, "ms_default": 14.0, "trials": 9}
+         "cta_walk": 1, "ms": 12.5, "ms_default": 14.0, "trials": 9}
     b = dict(a, tile_bits_log2=19, ms=11.0)
     dim3gpu.tuning_save(path, "p24_z20_w3", a)
     dim3gpu.tuning_save(path, "p20_z16_w5", dict(a, warp_slots_log2=9))

@@ -176,7 +176,7 @@ def test_batch_autotune_keeps_results_exact(built, golden):
     b = dim3gpu.Batch(c, pairs, specs)
     t = b.autotune(max_trials=6)
     assert 1 <= t["trials"] <= 6 and t["ms"] <= t["ms_default"]
-    assert c.get_param("cta_round_robin") == t["cta_round_robin"]
+    assert c.get_param("cta_walk") == t["cta_walk"]
     _check(golden, specs, b.run())
     b.close()
     c.close()

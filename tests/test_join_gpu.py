@@ -187,7 +187,7 @@ def test_autotune_applies_settings_and_keeps_results_exact(built, golden, tmp_pa
     assert key.startswith("p")
     t = c.autotune(dR, R.shape[0], dS, S.shape[0], max_trials=8)
     assert 1 <= t["trials"] <= 8 and t["ms"] <= t["ms_default"]
-    for k in ["tile_bits_log2", "block_threads", "block_slots_log2", "warp_slots_log2", "cta_round_robin"]:
+    for k in ["tile_bits_log2", "block_threads", "block_slots_log2", "warp_slots_log2", "cta_walk"]:
         assert c.get_param(k) == t[k]
     check_pairs(c.join_project(R, S), index[name], arrays, name)
     path = str(tmp_path / "t.txt")
