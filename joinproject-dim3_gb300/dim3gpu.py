@@ -632,6 +632,26 @@ def batch_params(seed, q, n_lo=1e4, n_hi=4e6, s_lo=0.5, s_hi=1.5, d_lo=1e3, d_hi
 
 
 # Named workloads (the bench and the tests use the same shapes).
+def fmix32_np(v):
+    """murmur3 fmix32 over a uint32 array (the A-tile and shard function)."""
+    v = np.asarray(v, dtype=np.uint32).astype(np.uint64)
+    v ^= v >> np.uint64(16)
+    v = (v * np.uint64(0x85ebca6b)) & np.uint64(0xFFFFFFFF)
+    v ^= v >> np.uint64(13)
+    v = (v * np.uint64(0xc2b2ae35)) & np.uint64(0xFFFFFFFF)
+    v ^= v >> np.uint64(16)
+    return v
+
+
+def a_shard(R, rank, world):
+    """Rows of R whose first value A falls in shard `rank` of `world`
+    (fmix32(A) mod world).  The multi-GPU form of the join-project: rank r
+    joins its shard of R with all of S; shards of the result are disjoint
+    (they partition the pairs by A), so no data is exchanged."""
+    R = np.asarray(R, dtype=np.uint32).reshape(-1, 2)
+    return np.ascontiguousarray(R[(fmix32_np(R[:, 0]) % np.uint64(world)) == np.uint64(rank)])
+
+
 def _zipf_sum_p2(dom, s):
     k = np.arange(1, dom + 1, dtype=np.float64)
     w = k ** -s

@@ -4,6 +4,7 @@
     python run_case.py --workload zipf12_16m --mode count_summary --tiles 16 --tile-hi 1
     python run_case.py --mode batch [--queries 512]          # the mixed batch, one CUDA graph
     python run_case.py --mode relset_pass [--scale 1.0]      # 64 requests over the served set
+    python run_case.py --workload zipf_1m --mode autotune    # the autotuner's choice for a workload
 
 Prints one JSON line.  Used for profiling single launches (`ncu ...
 python run_case.py ...`): --mode count runs the mapping, CSR and count pass
@@ -87,7 +88,7 @@ def main():
     ap.add_argument("--workload", default="chung_lu_20m")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--mode", default="count",
-                    choices=["count", "project", "aggregate", "count_summary", "batch", "relset_pass"])
+                    choices=["count", "project", "aggregate", "count_summary", "batch", "relset_pass", "autotune"])
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--param", action="append", default=[], help="name=value tuning knob")
     ap.add_argument("--tiles", type=int, default=16)
@@ -125,6 +126,11 @@ def main():
         for _ in range(args.repeat):
             ctx.join_project_device(dR, R.shape[0], dS, S.shape[0], out, n)
             res.append(ctx.stats())
+    elif args.mode == "autotune":
+        t = ctx.autotune(dR, R.shape[0], dS, S.shape[0])
+        print(json.dumps({"workload": args.workload, "mode": "autotune", "tuning": t}))
+        ctx.close()
+        return
     elif args.mode == "count_summary":
         for _ in range(args.repeat):
             sm = ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], args.tiles, args.tile_lo, args.tile_hi)
