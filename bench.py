@@ -16,8 +16,11 @@ output (~87 GB) are far larger than L2, so no flush is needed between steps.
 
 --impl reference times the reference's CPU algorithm (the oracle port of
 DIM3_parallel, all host threads) on a bounded A-slice of the same workload.
-Under torchrun every rank runs an independent replica (the path does not
-exchange data between GPUs); rank 0 prints the line.
+Under torchrun (N>1) the join is A-partitioned: rank r joins the rows of R
+whose A hashes to shard r (fmix32(a) mod N) with all of S.  The shards'
+outputs are disjoint, so no data moves between GPUs; `value` is the pairs of
+all ranks (one integer all-reduce after the timed region) over the slowest
+rank's time (total work fixed: strong scaling).  Rank 0 prints the line.
 """
 import argparse
 import json
@@ -182,6 +185,8 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     R, S = make_workload(args.workload)
+    if world > 1:
+        R = dim3gpu.a_shard(R, rank, world)
     nR, nS = R.shape[0], S.shape[0]
     ctx = dim3gpu.Context(local_rank)
     stream = torch.cuda.Stream()
@@ -221,11 +226,15 @@ def run_gpu(args, rank, world, local_rank):
     assert n == n_out
     launches = ctx.stats()["launches"] - launches0
     clocks = clk.summary()
+    n_all = n_out
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = n_out * world / (ms / 1e3) / 1e6
+        c = torch.tensor([n_out], dtype=torch.int64, device="cuda")
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        n_all = int(c.item())
+    value = n_all / (ms / 1e3) / 1e6
 
     # e2e through the host-buffer ABI: pinned R, S and output.
     e2e = None
@@ -247,7 +256,7 @@ def run_gpu(args, rank, world, local_rank):
             t = torch.tensor([e2e_s], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
-        e2e = {"value": round(n_out * world / e2e_s / 1e6, 3), "unit": UNIT,
+        e2e = {"value": round(n_all / e2e_s / 1e6, 3), "unit": UNIT,
                "h2d_bytes_per_step": int((nR + nS) * 8), "d2h_bytes_per_step": int(n_out * 8),
                "ms_per_step": round(e2e_s * 1e3, 3)}
     st = ctx.stats()
@@ -264,11 +273,11 @@ def run_gpu(args, rank, world, local_rank):
     traffic = args.traffic if args.traffic is not None else profiled_traffic("k_single_bitmap", args.workload)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "nR": int(nR), "nS": int(nS),
-                   "n_out": int(n_out), "out_j": int(st["out_j"]), "l2": "inputs 8(|R|+|S|) and output > L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "n_out": int(n_all), "out_j": int(st["out_j"]), "l2": "inputs 8(|R|+|S|) and output > L2; no flush",
+                   "parallelism": ("a_shard%d (R by fmix32(a) mod N, S whole)" % world) if world > 1 else "single"},
         "phases_ms": {k: round(v / args.steps, 3) for k, v in ms_phase.items()},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "kernel": "k_single_bitmap",
@@ -587,12 +596,11 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         run_reference(args, rank, world)
-    elif args.workload == "batch512":
-        run_batch(args, rank, world, local_rank)
-    elif args.workload == "count16m":
-        run_count16m(args, rank, world, local_rank)
-    elif args.workload == "serve64":
-        run_serve(args, rank, world, local_rank)
+    elif args.workload in ("batch512", "count16m", "serve64"):
+        # one-GPU forms: under torchrun rank 0 runs them alone (n_gpus 1)
+        if rank == 0:
+            {"batch512": run_batch, "count16m": run_count16m, "serve64": run_serve}[args.workload](
+                args, 0, 1, local_rank)
     else:
         run_gpu(args, rank, world, local_rank)
 
