@@ -59,6 +59,8 @@ typedef struct {
     float ms_write_cls[3];     /* write pass device ms per row kernel: bitmap, block, warp */
     uint64_t out_j_cls[3];     /* candidates (join tuples) per row kernel: bitmap, block, warp */
     uint64_t n_out_cls[3];     /* distinct pairs per row kernel (single pass): bitmap, block, warp */
+    float ms_dense[3];         /* dense block device ms: selection + operands, tensor-core product, light pass */
+    uint32_t dense_kp;         /* K of the dense product (heavy_y padded to 128) */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */
@@ -78,7 +80,12 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * "cta_walk" (how CTA rows share candidates among warps: 0 = the row's
  * segment table staged in shared memory and its candidates split evenly,
  * 1 = warps take whole 32-entry chunks in turn, 2 = every chunk split
- * across the warps). */
+ * across the warps), "dense_block" (the heavy rows' join through their
+ * heaviest join values as one boolean product on the tensor cores: 0 off,
+ * 1 when the cost model prefers it, 2 whenever its bitmap fits),
+ * "dense_k_max" (32..4096: most join values in that product),
+ * "dense_mem_mb" (bitmap budget of that product, default 16384: it takes as
+ * many heavy rows as their x z bitmap fits, the largest first). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */

@@ -24,6 +24,7 @@
 #include "aggregate.cuh"
 #include "internal.h"
 #include "common.cuh"
+#include "dense.cuh"
 #include "expand.cuh"
 #include "mapper.cuh"
 #include "mapping.cuh"
@@ -79,6 +80,9 @@ struct Params {
     bool ordered = false;     // two-pass, rows in x-id order
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
     uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split
+    uint32_t dense = 1;       // dense block on the tensor cores: 0 off, 1 by cost model, 2 whenever it fits
+    uint32_t dense_k_max = 1024;  // most join values in the dense product
+    uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -89,6 +93,7 @@ struct Scalars {
     unsigned long long nrows[6];   // rows per class (index = class)
     unsigned long long outj_cls[6];  // candidates per class (index = class)
     unsigned long long cursor_at[3]; // single-pass cursor after the bitmap / block / warp kernel
+    unsigned long long dense_base;   // single-pass start of the dense block's pairs (~0: past the capacity)
     unsigned int err;
     unsigned int next_row[4];      // dynamic row counters of the CTA classes
     unsigned int pad;
@@ -115,6 +120,7 @@ struct dim3g_ctx {
     Scalars* h_sc = nullptr;  // pinned
     cudaEvent_t ev[6] = {};
     cudaEvent_t evc[8] = {};  // per row-class kernel timing
+    cudaEvent_t evd[4] = {};  // dense block: selection, operands, product, light pass
     uint64_t launches = 0;  // kernels launched on this context since creation
 };
 
@@ -234,6 +240,208 @@ unsigned resident_grid(K kernel, int block, size_t smem, int sm) {
     return (unsigned)(per * sm);
 }
 
+// ------------------------------------------------------------ dense block
+// The heavy rows' (bitmap classes') join through their heaviest join values
+// as one boolean product on the tensor cores (dense.cuh).  Cost model, in
+// seconds, against the bitmap-class expansion it replaces (4 algorithmic
+// bytes per candidate):
+//   product   2 Mp Np Kp / kDenseFlops
+//   bitmap    written by the product, read by the light pass and emission
+//   light     the candidates through the other join values, kLightBytes each
+constexpr double kDenseFlops = 2.0e15;
+constexpr double kDenseBw = 6.0e12;
+constexpr double kSparseBw = 5.0e12;
+constexpr double kLightBytes = 40.0;
+constexpr uint64_t kDenseMinCand = (uint64_t)1 << 26;  // smaller heavy work stays sparse (cost model mode)
+
+struct DensePlan {
+    bool on = false;
+    uint32_t nd = 0;      // rows of the block: list_m[0 .. nd) (the bitmap classes' rows, huge ones first)
+    uint32_t Wd = 0;      // bitmap words per row (allocated)
+    uint32_t Wm = 0;      // bitmap words per row holding z < m
+    uint32_t cpr = 0;     // 32-word chunks per row
+    const uint32_t* D = nullptr;
+    const unsigned long long* coff = nullptr;  // nd * cpr + 1 chunk offsets (exclusive prefix of popcounts)
+};
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+// 2-D byte tensor of `rows` rows of Kp bytes; boxes of 128 bytes x box_rows,
+// 128-byte swizzle (the layout the product's descriptors expect).
+int dense_map(dim3g_ctx* c, CUtensorMap* map, void* base, uint64_t rows, uint32_t Kp, uint32_t box_rows) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return fail(c, DIM3G_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[2] = {Kp, rows};
+    const cuuint64_t strides[1] = {Kp};
+    const cuuint32_t box[2] = {kDenseBK, box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(c, DIM3G_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return DIM3G_OK;
+}
+
+uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+// Decides on and runs the dense block for a prefix of list_m (as many of
+// the bitmap classes' rows as the bitmap budget holds); on success with
+// dp->on the bitmap holds those rows' distinct z, and the device counts of
+// classes 3 and 4 add up to the rows left (list_m + nd onwards), which the
+// bitmap-class kernels then take.
+int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, const uint32_t* list_m, uint32_t k,
+              uint32_t m, DensePlan* dp) {
+    *dp = DensePlan{};
+    const uint32_t mode = c->prm.dense;
+    if (mode == 0 || jp.aggregate || jp.sum.tiles) return DIM3G_OK;
+    cudaStream_t st = c->stream;
+    const int sm = c->sm_count;
+    CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in row binning (flags %u)", c->h_sc->err);
+    const uint64_t n_heavy = c->h_sc->nrows[3] + c->h_sc->nrows[4];
+    const uint64_t cd_all = c->h_sc->outj_cls[3] + c->h_sc->outj_cls[4];
+    if (n_heavy == 0 || cd_all == 0) return DIM3G_OK;
+    if (mode == 1 && cd_all < kDenseMinCand) return DIM3G_OK;
+    const uint64_t Np = round_up(m, kDenseBN), Wd = Np / 32;
+    // rows the bitmap budget holds, whole 128-row tiles
+    const uint64_t fit = c->prm.dense_mem / (Wd * 4) / kDenseBM * kDenseBM;
+    const uint64_t nd = n_heavy < fit ? n_heavy : fit;
+    if (nd == 0) return DIM3G_OK;
+    const uint64_t Mp = round_up(nd, kDenseBM), dbytes = Mp * Wd * 4;
+    const double t_bitmap = 3.0 * (double)dbytes / kDenseBw;
+    const double t_min = 2.0 * Mp * Np * kDenseBK / kDenseFlops + t_bitmap;
+    if (mode == 1 && nd == n_heavy && t_min >= (double)cd_all * 4.0 / kSparseBw) return DIM3G_OK;
+
+    CU(cudaEventRecord(c->evd[0], st));
+    uint32_t* degd = ws_get<uint32_t>(c, k);
+    int32_t* hid = ws_get<int32_t>(c, k);
+    uint32_t* hy = ws_get<uint32_t>(c, c->prm.dense_k_max);
+    unsigned int* bin_n = ws_get<unsigned int>(c, kDenseBins + 1);  // [kDenseBins]: heavy-column counter
+    unsigned long long* bin_mass = ws_get<unsigned long long>(c, kDenseBins);
+    if (!degd || !hid || !hy || !bin_n || !bin_mass) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense)");
+    CU(cudaMemsetAsync(degd, 0, (size_t)k * 4, st));
+    CU(cudaMemsetAsync(bin_n, 0, (kDenseBins + 1) * 4, st));
+    CU(cudaMemsetAsync(bin_mass, 0, kDenseBins * 8, st));
+    // a sample of about 8192 heavy rows estimates the join values' mass
+    const uint32_t step = nd > 8192 ? (uint32_t)(nd / 8192) : 1u;
+    k_dense_deg<<<grid_for((nd / step + 1) * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, step, degd);
+    CHECK_LAUNCH();
+    k_dense_bins<<<grid_for(k, sm), 256, 0, st>>>(degd, rc.JR_S, rc.T, k, bin_n, bin_mass);
+    CHECK_LAUNCH();
+    std::vector<unsigned int> hn(kDenseBins);
+    std::vector<unsigned long long> hm(kDenseBins);
+    CU(cudaMemcpyAsync(hn.data(), bin_n, kDenseBins * 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hm.data(), bin_mass, kDenseBins * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    // the block's candidates: exact for all heavy rows, else the sample's
+    uint64_t cd = cd_all;
+    if (nd < n_heavy) {
+        cd = 0;
+        for (uint32_t b = 0; b < kDenseBins; b++) cd += hm[b] * step;
+    }
+    const double t_sparse = (double)cd * 4.0 / kSparseBw;
+    // the heavy join values: whole bins from the top, at most dense_k_max
+    // of them; the cut with the lowest modelled cost (mode 2: the most)
+    uint64_t kc = 0, heavy = 0, best_k = 0;
+    uint32_t best_cut = kDenseBins;
+    double best_t = 0;
+    for (int b = (int)kDenseBins - 1; b >= 0; b--) {
+        if (!hn[b]) continue;
+        if (kc + hn[b] > c->prm.dense_k_max) break;
+        kc += hn[b];
+        heavy += hm[b] * step;
+        const uint64_t Kp = round_up(kc, kDenseBK);
+        const double light = heavy >= cd ? 0.0 : (double)(cd - heavy);  // heavy is a sampled estimate
+        const double t = 2.0 * Mp * Np * Kp / kDenseFlops + t_bitmap + light * kLightBytes / kDenseBw;
+        if (mode == 2 || best_k == 0 || t < best_t) {
+            best_t = t;
+            best_k = kc;
+            best_cut = (uint32_t)b;
+        }
+    }
+    if (best_k == 0) return DIM3G_OK;
+    if (mode == 1 && best_t >= t_sparse) return DIM3G_OK;
+    const uint32_t Kp = (uint32_t)round_up(best_k, kDenseBK);
+    uint8_t* A = ws_get<uint8_t>(c, Mp * Kp);
+    uint8_t* B = ws_get<uint8_t>(c, Np * Kp);
+    uint32_t* D = ws_get<uint32_t>(c, Mp * Wd);
+    if (!A || !B || !D) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense operands)");
+    k_dense_hid<<<grid_for(k, sm), 256, 0, st>>>(degd, rc.JR_S, rc.T, k, best_cut, hid, hy, bin_n + kDenseBins);
+    CHECK_LAUNCH();
+    CU(cudaMemsetAsync(A, 0, Mp * Kp, st));
+    CU(cudaMemsetAsync(B, 0, Np * Kp, st));
+    k_dense_fill_a<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, hid, A, Kp);
+    CHECK_LAUNCH();
+    k_dense_fill_b<<<dim3(16, (unsigned)best_k), 256, 0, st>>>(rc.JR_S, rc.IC_S, rc.T, hy, B, Kp);
+    CHECK_LAUNCH();
+    CUtensorMap mA, mB;
+    int r = dense_map(c, &mA, A, Mp, Kp, kDenseBM);
+    if (!r) r = dense_map(c, &mB, B, Np, Kp, kDenseBN);
+    if (r) return r;
+    const uint32_t mt = (uint32_t)(Mp / kDenseBM), nt = (uint32_t)(Np / kDenseBN);
+    const uint64_t ntile = (uint64_t)mt * nt;
+    CU(cudaEventRecord(c->evd[1], st));
+    k_dense_mma<<<(unsigned)(ntile < (uint64_t)sm ? ntile : (uint64_t)sm), kDenseThreads, kDenseSmem, st>>>(
+        mA, mB, D, (uint32_t)Wd, mt, nt, Kp / kDenseBK, &sc->err);
+    CHECK_LAUNCH();
+    CU(cudaEventRecord(c->evd[2], st));
+    k_dense_light<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, rc.JR_S, rc.IC_S, rc.T, list_m,
+                                                         (uint32_t)nd, hid, D, (uint32_t)Wd);
+    CHECK_LAUNCH();
+    // chunk popcounts and their offsets
+    const uint32_t cpr = (uint32_t)((Wd + 31) / 32);
+    const uint64_t nc = nd * cpr;
+    uint32_t* cc = ws_get<uint32_t>(c, nc + 1);
+    unsigned long long* coff = ws_get<unsigned long long>(c, nc + 1);
+    uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(nc + 1));
+    if (!cc || !coff || !bsum) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense chunks)");
+    k_dense_chunks<<<grid_for(nc * 8, sm), 256, 0, st>>>((uint32_t)nd, D, (uint32_t)Wd, cpr, cc);
+    CHECK_LAUNCH();
+    SCAN(U32Src{cc}, OffDst{coff}, nc + 1, bsum, nullptr);
+    CU(cudaEventRecord(c->evd[3], st));
+    {
+        // the bitmap-class kernels take the rows after the block's
+        const unsigned long long rest[2] = {n_heavy - nd, 0};
+        CU(cudaMemcpyAsync(&sc->nrows[3], rest, sizeof rest, cudaMemcpyHostToDevice, st));
+        CU(cudaStreamSynchronize(st));  // `rest` is on this frame
+    }
+    c->stats.rows_dense = (uint32_t)nd;
+    c->stats.heavy_y = (uint32_t)best_k;
+    c->stats.dense_kp = Kp;
+    dp->on = true;
+    dp->nd = (uint32_t)nd;
+    dp->Wd = (uint32_t)Wd;
+    dp->Wm = (m + 31) / 32;
+    dp->cpr = cpr;
+    dp->D = D;
+    dp->coff = coff;
+    return DIM3G_OK;
+}
+
+// Device ms of the dense block's phases into the stats (after a sync).
+void dense_times(dim3g_ctx* c, const DensePlan& dp) {
+    if (!dp.on) return;
+    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&c->stats.ms_dense[i], c->evd[i], c->evd[i + 1]);
+}
+
 int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     cudaStream_t st = c->stream;
     c->ws.reset();
@@ -258,7 +466,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint2* Qk = ws_get<uint2>(c, jp.nQ);
     uint2* Pm = ws_get<uint2>(c, jp.nP);
     uint32_t* id2x = ws_get<uint32_t>(c, jp.nP);
-    uint32_t* id2z = ws_get<uint32_t>(c, jp.nQ);
+    uint32_t* id2z = ws_get<uint32_t>(c, round_up(jp.nQ, 1024) + 1024);  // whole 1024-id chunks (dense emission)
     uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(capP > capQ ? capP : capQ));
     if (!sc || !tx.slots || !ty.slots || !tz.slots || !Qk || !Pm || !id2x || !id2z || !bsum)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
@@ -374,9 +582,14 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     if (tiny) SCAN(ClassSrc{cls, 5}, ListDst{list_t, nullptr}, n, bsum2, &sc->nrows[5]);
     CU(cudaMemsetAsync(cnt, 0, ((uint64_t)n + 1) * 4, st));
     CU(cudaEventRecord(c->ev[2], st));
+    DensePlan dp;
+    {
+        int r = run_dense(c, jp, rc, sc, list_m, k, m, &dp);
+        if (r) return r;
+    }
 
     // Row counts are read on the device; grids are resident CTAs x SMs.
-    const RowLists L{list_w, list_b, list_m, &sc->nrows[1], &sc->nrows[2], &sc->nrows[3], &sc->nrows[4]};
+    const RowLists L{list_w, list_b, list_m + dp.nd, &sc->nrows[1], &sc->nrows[2], &sc->nrows[3], &sc->nrows[4]};
     rc.next_row = sc->next_row;
     const uint32_t wpc = warps_per_cta((size_t)4 << c->prm.warp_lg);  // warp-class CTA width
     const size_t smem_w = (size_t)wpc << c->prm.warp_lg << 2;
@@ -442,6 +655,13 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         const size_t ss_w = (size_t)wps * warp_row_words(c->prm.warp_lg, kStage) * 4;
         const uint32_t wpt = warps_per_cta(warp_row_words(kTinyLg, kTinyStage) * 4);
         const size_t ss_t = (size_t)wpt * warp_row_words(kTinyLg, kTinyStage) * 4;
+        if (dp.on) {
+            k_dense_reserve<<<1, 1, 0, st>>>(dp.coff + (uint64_t)dp.nd * dp.cpr, &sc->cursor, cap, &sc->dense_base);
+            CHECK_LAUNCH();
+            k_dense_emit<<<resident_grid(k_dense_emit, 256, kDenseEmitSmem, sm), 256, kDenseEmitSmem, st>>>(
+                list_m, dp.nd, dp.D, dp.Wd, dp.Wm, dp.cpr, dp.coff, id2x, id2z, out, nullptr, &sc->dense_base);
+            CHECK_LAUNCH();
+        }
         k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3, L.n4,
                                                                                          bm_words);
         CHECK_LAUNCH();
@@ -464,6 +684,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CU(cudaEventRecord(c->ev[3], st));
         CU(cudaStreamSynchronize(st));
         if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in single pass (flags %u)", c->h_sc->err);
+        dense_times(c, dp);
         const uint64_t total = c->h_sc->cursor;
         S.out_j = c->h_sc->outj;
         S.n_out_cls[0] = c->h_sc->cursor_at[0];
@@ -494,6 +715,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
 
     // count pass (the bitmap rows, the largest, start first)
     CU(cudaEventRecord(c->evc[0], st));
+    if (dp.on) {
+        k_dense_rowcnt<<<grid_for(dp.nd, sm), 256, 0, st>>>(list_m, dp.nd, dp.cpr, dp.coff, cnt);
+        CHECK_LAUNCH();
+    }
     k_rows_bitmap<false><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
     CHECK_LAUNCH();
     CU(cudaEventRecord(c->evc[1], st));
@@ -508,6 +733,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     CU(cudaEventRecord(c->ev[3], st));
     CU(cudaStreamSynchronize(st));
     if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in count pass (flags %u)", c->h_sc->err);
+    dense_times(c, dp);
     const uint64_t total = c->h_sc->total;
     for (int i = 0; i < 3; i++) cudaEventElapsedTime(&S.ms_count_cls[i], c->evc[i], c->evc[i + 1]);
     S.out_j = c->h_sc->outj;
@@ -542,6 +768,11 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
             if (r) return r;
         } else {
             CU(cudaEventRecord(c->evc[4], st));
+            if (dp.on) {
+                k_dense_emit<<<resident_grid(k_dense_emit, 256, kDenseEmitSmem, sm), 256, kDenseEmitSmem, st>>>(
+                    list_m, dp.nd, dp.D, dp.Wd, dp.Wm, dp.cpr, dp.coff, id2x, id2z, out, off, nullptr);
+                CHECK_LAUNCH();
+            }
             k_rows_bitmap<true><<<g_m, blk_m, smem_m, st>>>(rc, L.m, L.n3, L.n4);
             CHECK_LAUNCH();
             CU(cudaEventRecord(c->evc[5], st));
@@ -778,9 +1009,10 @@ int dim3g_create(int device, dim3g_ctx** out) {
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->evc) cudaEventCreate(&e);
+    for (auto& e : c->evd) cudaEventCreate(&e);
     c->stream = c->own_stream;
     // Shared-memory carve-outs for the expansion kernels (largest settings).
-    const int smem_w = 8 << 11 << 2, smem_b = 1 << 14 << 2, smem_m = (1 << 20) / 8;
+    const int smem_b = 1 << 14 << 2, smem_m = (1 << 20) / 8;
     const int smem_wmax = 200 * 1024;
     bool ok = cudaFuncSetAttribute(k_rows_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_wmax) == cudaSuccess &&
               cudaFuncSetAttribute(k_rows_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_wmax) == cudaSuccess &&
@@ -793,6 +1025,10 @@ int dim3g_create(int device, dim3g_ctx** out) {
                                    ((1 << 14) + 32 * (int)kStage) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_dense_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseSmem) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_dense_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseEmitSmem) ==
+                  cudaSuccess &&
               set_aggregate_attributes();
     if (!ok) {
         cudaGetLastError();
@@ -815,6 +1051,8 @@ void dim3g_destroy(dim3g_ctx* c) {
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : c->evc)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->evd)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
@@ -860,6 +1098,15 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "ordered_output")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "ordered_output must be 0 or 1");
         c->prm.ordered = v == 1;
+    } else if (!strcmp(name, "dense_block")) {
+        if (v < 0 || v > 2) return fail(c, DIM3G_ERR_INVALID, "dense_block must be 0, 1 or 2");
+        c->prm.dense = (uint32_t)v;
+    } else if (!strcmp(name, "dense_k_max")) {
+        if (v < 32 || v > 4096) return fail(c, DIM3G_ERR_INVALID, "dense_k_max must be in 32..4096");
+        c->prm.dense_k_max = (uint32_t)v;
+    } else if (!strcmp(name, "dense_mem_mb")) {
+        if (v < 1 || v > (1 << 20)) return fail(c, DIM3G_ERR_INVALID, "dense_mem_mb must be in 1..2^20");
+        c->prm.dense_mem = (uint64_t)v << 20;
     } else {
         return fail(c, DIM3G_ERR_INVALID, "unknown parameter %s", name);
     }
@@ -875,6 +1122,9 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "block_threads")) *v = c->prm.block_threads;
     else if (!strcmp(name, "host_direct_output")) *v = c->prm.host_direct ? 1 : 0;
     else if (!strcmp(name, "cta_walk")) *v = c->prm.cta_rr;
+    else if (!strcmp(name, "dense_block")) *v = c->prm.dense;
+    else if (!strcmp(name, "dense_k_max")) *v = c->prm.dense_k_max;
+    else if (!strcmp(name, "dense_mem_mb")) *v = (int64_t)(c->prm.dense_mem >> 20);
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

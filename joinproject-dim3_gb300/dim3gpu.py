@@ -46,13 +46,14 @@ class Stats(ctypes.Structure):
         ("ms_write", ctypes.c_float), ("ms_total", ctypes.c_float), ("launches", ctypes.c_uint64),
         ("ms_count_cls", ctypes.c_float * 3), ("ms_write_cls", ctypes.c_float * 3),
         ("out_j_cls", ctypes.c_uint64 * 3), ("n_out_cls", ctypes.c_uint64 * 3),
+        ("ms_dense", ctypes.c_float * 3), ("dense_kp", ctypes.c_uint32),
     ]
 
     def as_dict(self):
         d = {}
         for k, _ in self._fields_:
             v = getattr(self, k)
-            if k.startswith("ms_") and k.endswith("_cls"):
+            if k.startswith("ms_") and (k.endswith("_cls") or k == "ms_dense"):
                 v = [round(float(x), 3) for x in v]
             elif k.endswith("_cls"):
                 v = [int(x) for x in v]
