@@ -158,7 +158,7 @@ def run_reference(args, rank, world):
     sample = "1/%d A-slice of %s per step (full S), oracle port of DIM3_parallel" % (parts, args.workload)
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "sample": sample},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
@@ -205,7 +205,7 @@ def run_gpu(args, rank, world, local_rank):
             dist.barrier()
         torch.cuda.synchronize()
 
-    ms_write, ms_bitmap = [], []
+    ms_write, ms_bitmap, ms_mma = [], [], []
     ms_phase = {"ms_map": 0.0, "ms_csr": 0.0, "ms_count": 0.0, "ms_write": 0.0}
     launches0 = ctx.stats()["launches"]
     with ClockSampler(local_rank) as clk:
@@ -218,6 +218,7 @@ def run_gpu(args, rank, world, local_rank):
             st = ctx.stats()
             ms_write.append(st["ms_write"])
             ms_bitmap.append(st["ms_write_cls"][0])
+            ms_mma.append(st["ms_dense"][1])
             for k in ms_phase:
                 ms_phase[k] += st[k]
         ev1.record(stream)
@@ -261,16 +262,42 @@ def run_gpu(args, rank, world, local_rank):
                "ms_per_step": round(e2e_s * 1e3, 3)}
     st = ctx.stats()
     peak, peak_kind = load_peaks()
-    # Dominant kernel: k_single_bitmap (the heavy rows' single-pass
-    # expansion), timed by the library's CUDA events on its stream inside
-    # the timed region.  Algorithmic bytes per launch: 4 B per candidate z id
-    # read + 8 B per distinct pair written, over that kernel's rows.
     ms_b = sum(ms_bitmap) / len(ms_bitmap)
-    alg_bytes = 4 * st["out_j_cls"][0] + 8 * st["n_out_cls"][0]
+    dense = st["rows_dense"] > 0
+    if dense:
+        # The heavy rows went through the dense block: its dominant kernel is
+        # the emission (k_dense_emit), whose algorithmic bytes are the 8 B of
+        # every pair it writes (the bitmap it reads is < 2 % of that).
+        kernel = "k_dense_emit"
+        alg_bytes = 8 * st["n_out_cls"][0]
+    else:
+        # Dominant kernel: k_single_bitmap (the heavy rows' single-pass
+        # expansion), timed by the library's CUDA events on its stream inside
+        # the timed region.  Algorithmic bytes per launch: 4 B per candidate z
+        # id read + 8 B per distinct pair written, over that kernel's rows.
+        kernel = "k_single_bitmap"
+        alg_bytes = 4 * st["out_j_cls"][0] + 8 * st["n_out_cls"][0]
     achieved = alg_bytes / (ms_b / 1e3) / 1e9
     ms_w = sum(ms_write) / len(ms_write)
     alg_all = 4 * st["out_j"] + 8 * n_out
-    traffic = args.traffic if args.traffic is not None else profiled_traffic("k_single_bitmap", args.workload)
+    traffic = args.traffic if args.traffic is not None else profiled_traffic(kernel, args.workload)
+    tensor = None
+    if dense:
+        # the tensor-core product: 2 Mp Np Kp MMA flops per launch (padded
+        # tiles are executed), fp8 e4m3 operands, f32 accumulators
+        mp = (st["rows_dense"] + 127) // 128 * 128
+        np_ = (st["nz"] + 255) // 256 * 256
+        flops = 2 * mp * np_ * st["dense_kp"]
+        ms_t = sum(ms_mma) / len(ms_mma)
+        ach_t = flops / (ms_t / 1e3) / 1e12
+        bf16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops") \
+            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+        tensor = {"bound": "tensor", "kernel": "k_dense_mma", "achieved": round(ach_t, 1), "peak": 4500.0,
+                  "peak_kind": "nominal fp8 dense (the measured peaks are bf16 only)", "unit": "TFLOP/s",
+                  "frac": round(ach_t / 4500.0, 4),
+                  "vs_measured_bf16_burst": round(ach_t / bf16, 4) if bf16 else None,
+                  "flops_per_launch": int(flops), "ms_per_launch": round(ms_t, 3), "rows": st["rows_dense"],
+                  "heavy_y": st["heavy_y"], "kp": st["dense_kp"]}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "strong",
@@ -280,12 +307,13 @@ def run_gpu(args, rank, world, local_rank):
                    "parallelism": ("a_shard%d (R by fmix32(a) mod N, S whole)" % world) if world > 1 else "single"},
         "phases_ms": {k: round(v / args.steps, 3) for k, v in ms_phase.items()},
         "e2e": e2e,
-        "roofline": {"bound": "hbm", "kernel": "k_single_bitmap",
+        "roofline": {"bound": "hbm", "kernel": kernel,
                      "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(ms_b, 3),
                      "expansion_all_classes": {"alg_bytes": int(alg_all), "ms": round(ms_w, 3),
                                                "achieved": round(alg_all / (ms_w / 1e3) / 1e9, 1)}},
+        "roofline_tensor": tensor,
         "gpu_launches": launches,
         "clocks": clocks,
     }

@@ -61,6 +61,7 @@ typedef struct {
     uint64_t n_out_cls[3];     /* distinct pairs per row kernel (single pass): bitmap, block, warp */
     float ms_dense[3];         /* dense block device ms: selection + operands, tensor-core product, light pass */
     uint32_t dense_kp;         /* K of the dense product (heavy_y padded to 128) */
+    uint64_t dense_light;      /* candidates of the dense block's rows through light join values (estimate) */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */

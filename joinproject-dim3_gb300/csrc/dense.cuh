@@ -364,8 +364,13 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
 }
 
 // ------------------------------------------------------------ light pass
-// The light join values of every heavy row: their S rows' z are OR-ed into
+// The light join values of every block row: their S rows' z are OR-ed into
 // the row's bitmap (warp per row; an atomic only for a bit not yet set).
+// The row's entries are taken 32 at a time, one per lane (their S rows'
+// bounds loaded in parallel).  When the batch's light S rows average 32 z or
+// more, the warp streams them one after another; otherwise a warp prefix sum
+// over their lengths flattens the candidates, which the lanes take 32 at a
+// time, each finding its entry by a 5-step search over the prefix.
 static __global__ void k_dense_light(const uint32_t* __restrict__ JR_R, const uint32_t* __restrict__ IC_R,
                                      const uint32_t* __restrict__ JR_S, const uint32_t* __restrict__ IC_S, uint32_t T,
                                      const uint32_t* __restrict__ rows, uint32_t nd, const int32_t* __restrict__ hid,
@@ -375,14 +380,52 @@ static __global__ void k_dense_light(const uint32_t* __restrict__ JR_R, const ui
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nd; i += nw) {
         const uint32_t x = rows[i];
         uint32_t* Di = D + (size_t)i * Wd;
-        for (uint32_t e = JR_R[x]; e < JR_R[x + 1]; e++) {
-            const uint32_t y = IC_R[e];
-            if (hid[y] >= 0) continue;
-            const uint32_t e1 = JR_S[(unsigned long long)(y + 1) * T];
-            for (uint32_t j = JR_S[(unsigned long long)y * T] + lane; j < e1; j += 32) {
-                const uint32_t z = IC_S[j];
-                const uint32_t bit = 1u << (z & 31);
-                if (!(Di[z >> 5] & bit)) atomicOr(&Di[z >> 5], bit);
+        const uint32_t e1 = JR_R[x + 1];
+        for (uint32_t eb = JR_R[x]; eb < e1; eb += 32) {
+            const uint32_t e = eb + lane;
+            uint32_t s0 = 0, len = 0;
+            if (e < e1) {
+                const uint32_t y = IC_R[e];
+                if (hid[y] < 0) {
+                    s0 = JR_S[(unsigned long long)y * T];
+                    len = JR_S[(unsigned long long)(y + 1) * T] - s0;
+                }
+            }
+            uint32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += v;
+            }
+            const uint32_t excl = incl - len;
+            const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+            uint32_t lights = __ballot_sync(0xffffffffu, len != 0);
+            if (tot >= 32u * __popc(lights)) {
+                while (lights) {
+                    const uint32_t l = __ffs(lights) - 1;
+                    lights &= lights - 1;
+                    const uint32_t os = __shfl_sync(0xffffffffu, s0, l), n = __shfl_sync(0xffffffffu, len, l);
+                    for (uint32_t j = lane; j < n; j += 32) {
+                        const uint32_t z = IC_S[os + j];
+                        const uint32_t bit = 1u << (z & 31);
+                        if (!(Di[z >> 5] & bit)) atomicOr(&Di[z >> 5], bit);
+                    }
+                }
+                continue;
+            }
+            for (uint32_t j0 = 0; j0 < tot; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                uint32_t pos = 0;  // first lane whose inclusive prefix exceeds j
+#pragma unroll
+                for (uint32_t st = 16; st > 0; st >>= 1)
+                    if (__shfl_sync(0xffffffffu, incl, pos + st - 1) <= j) pos += st;
+                const uint32_t os = __shfl_sync(0xffffffffu, s0, pos);
+                const uint32_t oe = __shfl_sync(0xffffffffu, excl, pos);
+                if (j < tot) {
+                    const uint32_t z = IC_S[os + (j - oe)];
+                    const uint32_t bit = 1u << (z & 31);
+                    if (!(Di[z >> 5] & bit)) atomicOr(&Di[z >> 5], bit);
+                }
             }
         }
     }

@@ -11,6 +11,7 @@
 // (Hybrid_solution, dim3.hpp:889-974).  Two host synchronisations: one for
 // the id domain sizes, one for the output size.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -245,10 +246,15 @@ unsigned resident_grid(K kernel, int block, size_t smem, int sm) {
 // as one boolean product on the tensor cores (dense.cuh).  Cost model, in
 // seconds, against the bitmap-class expansion it replaces (4 algorithmic
 // bytes per candidate):
-//   product   2 Mp Np Kp / kDenseFlops
+//   product   tiles per SM x max(kDenseTileS, MMA time of a tile at
+//             kDenseSmFlops); the fixed part is a tile's TMA fill and
+//             epilogue, which the MMAs hide from about Kp = 384 on
 //   bitmap    written by the product, read by the light pass and emission
 //   light     the candidates through the other join values, kLightBytes each
-constexpr double kDenseFlops = 2.0e15;
+// (constants measured on GB300, zipf_1m: 0.8 us a tile at Kp <= 256, about
+// 3.8 PFLOP/s for Kp = 384 .. 1024; the light pass 3-6 ps a candidate).
+constexpr double kDenseTileS = 0.8e-6;
+constexpr double kDenseSmFlops = 3.8e15 / 152;
 constexpr double kDenseBw = 6.0e12;
 constexpr double kSparseBw = 5.0e12;
 constexpr double kLightBytes = 40.0;
@@ -327,8 +333,14 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     if (nd == 0) return DIM3G_OK;
     const uint64_t Mp = round_up(nd, kDenseBM), dbytes = Mp * Wd * 4;
     const double t_bitmap = 3.0 * (double)dbytes / kDenseBw;
-    const double t_min = 2.0 * Mp * Np * kDenseBK / kDenseFlops + t_bitmap;
-    if (mode == 1 && nd == n_heavy && t_min >= (double)cd_all * 4.0 / kSparseBw) return DIM3G_OK;
+    const double tiles_per_sm = ceil((double)(Mp / kDenseBM) * (double)(Np / kDenseBN) / sm);
+    auto t_product = [&](uint64_t Kp) {
+        const double t_mma = 2.0 * kDenseBM * kDenseBN * (double)Kp / kDenseSmFlops;
+        return tiles_per_sm * (t_mma > kDenseTileS ? t_mma : kDenseTileS);
+    };
+    const double t_min = t_product(kDenseBK) + t_bitmap;
+    // the sparse cost of all heavy rows bounds that of any prefix of them
+    if (mode == 1 && t_min >= (double)cd_all * 4.0 / kSparseBw) return DIM3G_OK;
 
     CU(cudaEventRecord(c->evd[0], st));
     uint32_t* degd = ws_get<uint32_t>(c, k);
@@ -351,30 +363,31 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     CU(cudaMemcpyAsync(hn.data(), bin_n, kDenseBins * 4, cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(hm.data(), bin_mass, kDenseBins * 8, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    // the block's candidates: exact for all heavy rows, else the sample's
-    uint64_t cd = cd_all;
-    if (nd < n_heavy) {
-        cd = 0;
-        for (uint32_t b = 0; b < kDenseBins; b++) cd += hm[b] * step;
-    }
-    const double t_sparse = (double)cd * 4.0 / kSparseBw;
+    // the block's candidates: exact for all heavy rows, else the sample's;
+    // the light candidates of a cut are the sample's mass below it
+    double sampled = 0;
+    for (uint32_t b = 0; b < kDenseBins; b++) sampled += (double)hm[b] * step;
+    const double cd = nd < n_heavy ? sampled : (double)cd_all;
+    const double t_sparse = cd * 4.0 / kSparseBw;
     // the heavy join values: whole bins from the top, at most dense_k_max
     // of them; the cut with the lowest modelled cost (mode 2: the most)
-    uint64_t kc = 0, heavy = 0, best_k = 0;
+    uint64_t kc = 0, best_k = 0;
+    double heavy = 0;
     uint32_t best_cut = kDenseBins;
-    double best_t = 0;
+    double best_t = 0, best_light = 0;
     for (int b = (int)kDenseBins - 1; b >= 0; b--) {
         if (!hn[b]) continue;
         if (kc + hn[b] > c->prm.dense_k_max) break;
         kc += hn[b];
-        heavy += hm[b] * step;
+        heavy += (double)hm[b] * step;
         const uint64_t Kp = round_up(kc, kDenseBK);
-        const double light = heavy >= cd ? 0.0 : (double)(cd - heavy);  // heavy is a sampled estimate
-        const double t = 2.0 * Mp * Np * Kp / kDenseFlops + t_bitmap + light * kLightBytes / kDenseBw;
+        const double light = sampled > heavy ? sampled - heavy : 0.0;
+        const double t = t_product(Kp) + t_bitmap + light * kLightBytes / kDenseBw;
         if (mode == 2 || best_k == 0 || t < best_t) {
             best_t = t;
             best_k = kc;
             best_cut = (uint32_t)b;
+            best_light = light;
         }
     }
     if (best_k == 0) return DIM3G_OK;
@@ -426,6 +439,7 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     c->stats.rows_dense = (uint32_t)nd;
     c->stats.heavy_y = (uint32_t)best_k;
     c->stats.dense_kp = Kp;
+    c->stats.dense_light = (uint64_t)best_light;
     dp->on = true;
     dp->nd = (uint32_t)nd;
     dp->Wd = (uint32_t)Wd;

@@ -55,3 +55,25 @@ def test_tuning_cache_roundtrip(built, tmp_path):
     assert dim3gpu.tuning_load(path, "nope") is None
     with pytest.raises(dim3gpu.Dim3GError):
         dim3gpu.tuning_save(path, "has space", a)
+
+
+def test_stats_struct_matches_header(tmp_path):
+    """The ctypes mirror of dim3g_stats has the header struct's size and
+    field offsets (a C probe compiled against include/dim3gpu.h)."""
+    import shutil
+    import subprocess
+    import ctypes
+    import dim3gpu
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    fields = [f for f, _ in dim3gpu.Stats._fields_]
+    src = tmp_path / "probe.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"dim3gpu.h\"\nint main(void){\n"
+                   "printf(\"%zu\\n\", sizeof(dim3g_stats));\n"
+                   + "".join("printf(\"%%zu\\n\", offsetof(dim3g_stats, %s));\n" % f for f in fields) + "return 0;}\n")
+    exe = tmp_path / "probe"
+    subprocess.check_call(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    assert got[0] == ctypes.sizeof(dim3gpu.Stats)
+    assert got[1:] == [getattr(dim3gpu.Stats, f).offset for f in fields]
