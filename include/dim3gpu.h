@@ -62,6 +62,10 @@ typedef struct {
     float ms_dense[3];         /* dense block device ms: selection + operands, tensor-core product, light pass */
     uint32_t dense_kp;         /* K of the dense product (heavy_y padded to 128) */
     uint64_t dense_light;      /* candidates of the dense block's rows through light join values (estimate) */
+    uint32_t dense_skip;       /* why the dense block did not run: 0 it ran, 1 off or materialised COUNT, 2 no or
+                                  too little heavy work, 3 no budget, 4 cost model, 5 a multiplicity above 16
+                                  (summaries), 6 light buckets too large (summaries) */
+    uint32_t dense_bucket_max; /* largest per-tile light bucket (summaries) */
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */

@@ -35,7 +35,8 @@ constexpr uint32_t kDenseStages = 4;
 constexpr uint32_t kDenseAStage = kDenseBM * kDenseBK;  // 16 KB
 constexpr uint32_t kDenseBStage = kDenseBN * kDenseBK;  // 32 KB
 constexpr uint32_t kDenseSmem = kDenseStages * (kDenseAStage + kDenseBStage) + 1024 + 256;
-constexpr uint32_t kDenseThreads = 320;  // TMA warp, MMA warp, 8 epilogue warps
+constexpr uint32_t kDenseThreads = 320;     // bitmap mode: TMA warp, MMA warp, 8 epilogue warps
+constexpr uint32_t kDenseSumThreads = 576;  // summary modes: 16 epilogue warps (the group hashes are ALU work)
 constexpr uint32_t kDenseTmemCols = 2 * kDenseBN;  // two accumulators
 constexpr uint32_t kDenseBins = 512;               // candidate-mass bins: 8 per octave
 constexpr uint8_t kFp8One = 0x38;                  // e4m3 1.0
@@ -122,6 +123,45 @@ static __global__ void k_dense_fill_b(const uint32_t* __restrict__ JR_S, const u
     for (uint32_t e = JR_S[(unsigned long long)y * T] + blockIdx.x * blockDim.x + threadIdx.x; e < e1;
          e += gridDim.x * blockDim.x)
         B[(size_t)IC_S[e] * Kp + h] = kFp8One;
+}
+
+// Summary modes: the product counts join tuples, so the operands hold
+// multiplicities (duplicate tuples count): first as 32-bit counts, then
+// as e4m3 codes, exact for integers up to 16 (a larger multiplicity sets
+// *flag and the caller keeps the sparse path).
+static __global__ void k_dense_cnt_a(const uint32_t* __restrict__ JR_R, const uint32_t* __restrict__ IC_R,
+                                     const uint32_t* __restrict__ rows, uint32_t nd, const int32_t* __restrict__ hid,
+                                     uint32_t* __restrict__ A32, uint32_t Kp) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nd; i += nw) {
+        const uint32_t x = rows[i];
+        for (uint32_t e = JR_R[x] + lane; e < JR_R[x + 1]; e += 32) {
+            const int32_t h = hid[IC_R[e]];
+            if (h >= 0) atomicAdd(&A32[(size_t)i * Kp + h], 1u);
+        }
+    }
+}
+static __global__ void k_dense_cnt_b(const uint32_t* __restrict__ JR_S, const uint32_t* __restrict__ IC_S, uint32_t T,
+                                     const uint32_t* __restrict__ hy, uint32_t* __restrict__ B32, uint32_t Kp) {
+    const uint32_t h = blockIdx.y, y = hy[h];
+    const uint32_t e1 = JR_S[(unsigned long long)(y + 1) * T];
+    for (uint32_t e = JR_S[(unsigned long long)y * T] + blockIdx.x * blockDim.x + threadIdx.x; e < e1;
+         e += gridDim.x * blockDim.x)
+        atomicAdd(&B32[(size_t)IC_S[e] * Kp + h], 1u);
+}
+__device__ __forceinline__ uint8_t e4m3_of(uint32_t v) {  // exact for v <= 16
+    if (v == 0) return 0;
+    const uint32_t e = 31 - __clz(v);
+    return (uint8_t)(((e + 7) << 3) | (((v << 3) >> e) & 7u));
+}
+static __global__ void k_dense_to_fp8(const uint32_t* __restrict__ src, uint8_t* __restrict__ dst, size_t n,
+                                      uint32_t* flag) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t v = src[i];
+        if (v > 16) *flag = 1;
+        dst[i] = e4m3_of(v);
+    }
 }
 
 // ------------------------------------------------ PTX: mbarrier, TMA, tcgen05
@@ -216,11 +256,125 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 }
 
 // ------------------------------------------------------------ the product
-// D[i][z / 32] bit z % 32 = (A_i . B_z > 0) for i < mt * 128, z < nt * 256;
-// D has Wd 32-bit words per row (Wd >= nt * 8).  nk = K bytes / 128.
-static __global__ void __launch_bounds__(kDenseThreads, 1)
+// Epilogue modes: the bitmap (join-project), or per-A-tile summaries of the
+// groups (join-project summary: pair hashes; COUNT summary: group hashes of
+// the exact counts) with each tile's light candidates added in.
+enum DenseMode : int { kDenseBits = 0, kDenseSumProject = 1, kDenseSumCount = 2 };
+
+struct DenseSum {
+    const uint32_t* rows;  // block rows (x ids)
+    uint32_t nd;
+    const uint32_t* id2x;
+    const uint32_t* id2z;
+    const uint32_t* toff;  // light candidates of tile t: lb[toff[t] .. toff[t + 1])
+    const uint16_t* lb;    // (row in tile << 8) | (z in tile)
+    SumAcc sum;
+};
+
+// Adds a group's summary terms; light corrections replace a group's count.
+template <int kMode>
+__device__ __forceinline__ void dense_group(uint32_t a, uint32_t c, uint32_t cnt, unsigned long long& g,
+                                            unsigned long long& cs, unsigned long long& h) {
+    g += 1;
+    if (kMode == kDenseSumCount) {
+        cs += cnt;
+        h += group_hash(a, c, cnt);
+    } else {
+        cs += 1;
+        h += pair_hash(a, c);
+    }
+}
+
+// Summary of one 32-column chunk of a tile row: the product's counts v,
+// then the tile's light candidates of this row and chunk (each distinct
+// (row, z) once, with the number of its entries as its light count).
+template <int kMode>
+__device__ __forceinline__ void dense_sum_chunk(const uint32_t (&v)[32], const DenseSum& ds, uint32_t a, uint32_t z0,
+                                                uint32_t key0, uint32_t l0, uint32_t l1, unsigned long long& g,
+                                                unsigned long long& cs, unsigned long long& h) {
+    // branch-free over the 32 columns so their hash chains interleave; the
+    // chunk's z values 4 at a time in vector loads (z0 is a multiple of 32)
+#pragma unroll
+    for (uint32_t q = 0; q < 8; q++) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(ds.id2z + z0) + q);
+        const uint32_t zq[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (uint32_t r = 0; r < 4; r++) {
+            const uint32_t cnt = (uint32_t)__uint_as_float(v[4 * q + r]);
+            const bool p = cnt != 0;
+            const unsigned long long hv =
+                kMode == kDenseSumCount ? group_hash(a, zq[r], cnt) : pair_hash(a, zq[r]);
+            h += p ? hv : 0ull;
+            g += p;
+            cs += kMode == kDenseSumCount ? cnt : (uint32_t)p;
+        }
+    }
+    for (uint32_t k = l0; k < l1; k++) {
+        const uint32_t e = ds.lb[k];
+        if ((e & ~31u) != key0) continue;  // another row or chunk
+        uint32_t L = 0;
+        bool first = true;
+        for (uint32_t k2 = l0; k2 < l1; k2++)
+            if (ds.lb[k2] == e) {
+                L++;
+                if (k2 < k) first = false;
+            }
+        if (!first) continue;
+        const uint32_t u = e & 31;
+        uint32_t bv = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < 32; w++) bv = w == u ? v[w] : bv;
+        const uint32_t base = (uint32_t)__uint_as_float(bv);
+        const uint32_t c = ds.id2z[z0 + u];
+        if (kMode == kDenseSumCount) {
+            if (base) {
+                h -= group_hash(a, c, base);
+                g -= 1;
+                cs -= base;
+            }
+            dense_group<kMode>(a, c, base + L, g, cs, h);
+        } else if (!base) {
+            dense_group<kMode>(a, c, 1, g, cs, h);
+        }
+    }
+}
+
+// Adds a lane's sums to its row's A-tile (warp-reduced when the warp's
+// rows share one tile).
+__device__ __forceinline__ void dense_sum_flush(const SumAcc& sum, uint32_t tile, unsigned long long g,
+                                                unsigned long long cs, unsigned long long h) {
+    const uint32_t t0 = __shfl_sync(0xffffffffu, tile, 0);
+    if (__all_sync(0xffffffffu, tile == t0)) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            g += __shfl_xor_sync(0xffffffffu, g, o);
+            cs += __shfl_xor_sync(0xffffffffu, cs, o);
+            h += __shfl_xor_sync(0xffffffffu, h, o);
+        }
+        if ((threadIdx.x & 31) == 0 && g) {
+            unsigned long long* t = sum.tiles + 3ull * t0;
+            atomicAdd(&t[0], g);
+            atomicAdd(&t[1], cs);
+            atomicAdd(&t[2], h);
+        }
+    } else if (g) {
+        unsigned long long* t = sum.tiles + 3ull * tile;
+        atomicAdd(&t[0], g);
+        atomicAdd(&t[1], cs);
+        atomicAdd(&t[2], h);
+    }
+}
+
+// kDenseBits: D[i][z / 32] bit z % 32 = (A_i . B_z > 0) for i < mt * 128,
+// z < nt * 256; D has Wd 32-bit words per row (Wd >= nt * 8).  Summary
+// modes: the groups of block rows i < ds.nd go into ds.sum; tiles are taken
+// row-block-major so an epilogue thread keeps its row across ~nt / grid
+// consecutive tiles.  nk = K bytes / 128.
+template <int kMode>
+static __global__ void __launch_bounds__(kMode == kDenseBits ? kDenseThreads : kDenseSumThreads, 1)
     k_dense_mma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                uint32_t* __restrict__ D, uint32_t Wd, uint32_t mt, uint32_t nt, uint32_t nk, uint32_t* err) {
+                uint32_t* __restrict__ D, uint32_t Wd, uint32_t mt, uint32_t nt, uint32_t nk, uint32_t* err,
+                const DenseSum ds) {
     extern __shared__ uint8_t dsm_raw[];
     const uint32_t raw = smem_addr(dsm_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;  // 128-byte swizzle tiles sit on 1 KB boundaries
@@ -242,7 +396,7 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
         }
         for (uint32_t b = 0; b < 2; b++) {
             mbar_init(tfull + 8 * b, 1);
-            mbar_init(tempty + 8 * b, kDenseThreads - 64);
+            mbar_init(tempty + 8 * b, blockDim.x - 64);
         }
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -265,7 +419,7 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
         // producer: A and B tiles of every K block into the ring
         uint32_t s = 0, ph = 0;
         for (uint32_t t = blockIdx.x; t < ntile && !bad; t += gridDim.x) {
-            const uint32_t mi = t % mt, ni = t / mt;
+            const uint32_t mi = kMode == kDenseBits ? t % mt : t / nt, ni = kMode == kDenseBits ? t / mt : t % nt;
             for (uint32_t kb = 0; kb < nk; kb++) {
                 if (!mbar_wait(empty + 8 * s, ph ^ 1, abort)) {
                     bad = true;
@@ -315,18 +469,63 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
         }
     } else if (warp >= 2) {
         // epilogue: warp w reads TMEM lanes 32q..32q+31 (q = w % 4; a warp
-        // may only reach its own quadrant) and half hc of the columns
+        // may only reach its own quadrant) and part hc of the columns: halves
+        // (8 epilogue warps) or quarters (16)
         const uint32_t q = warp & 3, hc = (warp - 2) >> 2;
+        const uint32_t parts = (blockDim.x - 64) / 128, pcols = kDenseBN / parts;
         const uint32_t row = q * 32 + lane;
         uint32_t tb = 0, tph = 0;
+        // summary state: this lane's row (block row cur_mi * 128 + row)
+        uint32_t cur_mi = ~0u, a = 0, stile = 0;
+        bool live = false;
+        unsigned long long g = 0, cs = 0, h = 0;
         for (uint32_t t = blockIdx.x; t < ntile && !bad; t += gridDim.x) {
-            const uint32_t mi = t % mt, ni = t / mt;
+            const uint32_t mi = kMode == kDenseBits ? t % mt : t / nt, ni = kMode == kDenseBits ? t / mt : t % nt;
+            __syncwarp();
+            if (kMode != kDenseBits && mi != cur_mi) {
+                // a new row block: the sums are per A-tile, so a lane keeps
+                // accumulating while its rows stay in one tile; flush when
+                // some lane with sums moves to another
+                const uint32_t i = mi * kDenseBM + row;
+                const bool nlive = i < ds.nd;
+                const uint32_t na = nlive ? ds.id2x[ds.rows[i]] : 0u;
+                const uint32_t ntl = nlive ? ds.sum.tile(na) : 0u;
+                if (!__all_sync(0xffffffffu, !g || !nlive || ntl == stile)) {
+                    dense_sum_flush(ds.sum, stile, g, cs, h);
+                    g = cs = h = 0;
+                }
+                if (nlive) stile = ntl;
+                cur_mi = mi;
+                a = na;
+                live = nlive;
+            }
             // warp-uniform outcome: the TMEM loads below are warp-collective
             if (!__all_sync(0xffffffffu, mbar_wait(tfull + 8 * tb, tph, abort))) {
                 bad = true;
                 break;
             }
             tc_fence_after();
+            if (kMode != kDenseBits) {
+                const uint32_t l0 = ds.toff[t], l1 = ds.toff[t + 1];
+#pragma unroll 1
+                for (uint32_t j = 0; j < pcols / 32; j++) {
+                    uint32_t v[32];
+                    __syncwarp();  // tcgen05.ld is warp-collective; the sums before it diverge
+                    tmem_ld32(tmem + ((q * 32) << 16) + tb * kDenseBN + hc * pcols + j * 32, v);
+                    if (j == pcols / 32 - 1) {
+                        tc_fence_before();
+                        mbar_arrive(tempty + 8 * tb);  // the accumulator is in registers
+                    }
+                    if (live)
+                        dense_sum_chunk<kMode>(v, ds, a, ni * kDenseBN + hc * pcols + j * 32,
+                                               (row << 8) | (hc * pcols + j * 32), l0, l1, g, cs, h);
+                }
+                if (++tb == 2) {
+                    tb = 0;
+                    tph ^= 1;
+                }
+                continue;
+            }
             uint32_t w[kDenseBN / 64];
 #pragma unroll
             for (uint32_t j = 0; j < kDenseBN / 64; j++) {
@@ -346,6 +545,8 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
                 tph ^= 1;
             }
         }
+        __syncwarp();
+        if (kMode != kDenseBits && !bad) dense_sum_flush(ds.sum, stile, g, cs, h);
     }
     if (bad) {
         *abort = 1;
@@ -371,15 +572,53 @@ static __global__ void __launch_bounds__(kDenseThreads, 1)
 // more, the warp streams them one after another; otherwise a warp prefix sum
 // over their lengths flattens the candidates, which the lanes take 32 at a
 // time, each finding its entry by a 5-step search over the prefix.
+// The largest bucket of light candidates (summaries apply a tile's bucket
+// in the epilogue, each epilogue thread scanning it, so it must be small).
+constexpr uint32_t kDenseBucketMax = 64;
+static __global__ void k_dense_maxcnt(const uint32_t* __restrict__ tcnt, uint64_t n, unsigned int* out) {
+    uint32_t m = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        m = tcnt[i] > m ? tcnt[i] : m;
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// The visitor takes every light candidate (block row i, z id).
+struct LightOr {  // join-project: into the bitmap
+    uint32_t* D;
+    uint32_t Wd;
+    __device__ __forceinline__ void operator()(uint32_t i, uint32_t z) const {
+        uint32_t* w = D + (size_t)i * Wd + (z >> 5);
+        const uint32_t bit = 1u << (z & 31);
+        if (!(*w & bit)) atomicOr(w, bit);
+    }
+};
+struct LightCount {  // summaries: candidates per product tile
+    uint32_t* tcnt;
+    uint32_t nt;
+    __device__ __forceinline__ void operator()(uint32_t i, uint32_t z) const {
+        atomicAdd(&tcnt[(size_t)(i / kDenseBM) * nt + z / kDenseBN], 1u);
+    }
+};
+struct LightScatter {  // summaries: candidates into their tile's bucket
+    uint32_t* tcur;
+    uint16_t* lb;
+    uint32_t nt;
+    __device__ __forceinline__ void operator()(uint32_t i, uint32_t z) const {
+        const uint32_t p = atomicAdd(&tcur[(size_t)(i / kDenseBM) * nt + z / kDenseBN], 1u);
+        lb[p] = (uint16_t)(((i % kDenseBM) << 8) | (z % kDenseBN));
+    }
+};
+
+template <class V>
 static __global__ void k_dense_light(const uint32_t* __restrict__ JR_R, const uint32_t* __restrict__ IC_R,
                                      const uint32_t* __restrict__ JR_S, const uint32_t* __restrict__ IC_S, uint32_t T,
                                      const uint32_t* __restrict__ rows, uint32_t nd, const int32_t* __restrict__ hid,
-                                     uint32_t* __restrict__ D, uint32_t Wd) {
+                                     V visit) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nd; i += nw) {
         const uint32_t x = rows[i];
-        uint32_t* Di = D + (size_t)i * Wd;
         const uint32_t e1 = JR_R[x + 1];
         for (uint32_t eb = JR_R[x]; eb < e1; eb += 32) {
             const uint32_t e = eb + lane;
@@ -405,11 +644,7 @@ static __global__ void k_dense_light(const uint32_t* __restrict__ JR_R, const ui
                     const uint32_t l = __ffs(lights) - 1;
                     lights &= lights - 1;
                     const uint32_t os = __shfl_sync(0xffffffffu, s0, l), n = __shfl_sync(0xffffffffu, len, l);
-                    for (uint32_t j = lane; j < n; j += 32) {
-                        const uint32_t z = IC_S[os + j];
-                        const uint32_t bit = 1u << (z & 31);
-                        if (!(Di[z >> 5] & bit)) atomicOr(&Di[z >> 5], bit);
-                    }
+                    for (uint32_t j = lane; j < n; j += 32) visit(i, IC_S[os + j]);
                 }
                 continue;
             }
@@ -421,11 +656,7 @@ static __global__ void k_dense_light(const uint32_t* __restrict__ JR_R, const ui
                     if (__shfl_sync(0xffffffffu, incl, pos + st - 1) <= j) pos += st;
                 const uint32_t os = __shfl_sync(0xffffffffu, s0, pos);
                 const uint32_t oe = __shfl_sync(0xffffffffu, excl, pos);
-                if (j < tot) {
-                    const uint32_t z = IC_S[os + (j - oe)];
-                    const uint32_t bit = 1u << (z & 31);
-                    if (!(Di[z >> 5] & bit)) atomicOr(&Di[z >> 5], bit);
-                }
+                if (j < tot) visit(i, IC_S[os + (j - oe)]);
             }
         }
     }

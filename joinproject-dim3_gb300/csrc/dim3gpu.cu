@@ -82,7 +82,7 @@ struct Params {
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
     uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split
     uint32_t dense = 1;       // dense block on the tensor cores: 0 off, 1 by cost model, 2 whenever it fits
-    uint32_t dense_k_max = 1024;  // most join values in the dense product
+    uint32_t dense_k_max = 2048;  // most join values in the dense product
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
 };
 
@@ -254,6 +254,10 @@ unsigned resident_grid(K kernel, int block, size_t smem, int sm) {
 // (constants measured on GB300, zipf_1m: 0.8 us a tile at Kp <= 256, about
 // 3.8 PFLOP/s for Kp = 384 .. 1024; the light pass 3-6 ps a candidate).
 constexpr double kDenseTileS = 0.8e-6;
+// summary epilogue, measured on the 16M x 16M Zipf-1.2 COUNT: ~32K group
+// hashes a tile (11.1 us) + 0.34 us per light candidate in the tile's bucket
+constexpr double kDenseTileSumS = 11.1e-6;
+constexpr double kDenseBucketS = 0.34e-6;
 constexpr double kDenseSmFlops = 3.8e15 / 152;
 constexpr double kDenseBw = 6.0e12;
 constexpr double kSparseBw = 5.0e12;
@@ -316,7 +320,12 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
               uint32_t m, DensePlan* dp) {
     *dp = DensePlan{};
     const uint32_t mode = c->prm.dense;
-    if (mode == 0 || jp.aggregate || jp.sum.tiles) return DIM3G_OK;
+    // materialised COUNT output stays on the sparse kernels
+    uint32_t& skip = c->stats.dense_skip;
+    skip = 1;  // off, or materialised COUNT
+    if (mode == 0 || (jp.aggregate && !jp.sum.tiles)) return DIM3G_OK;
+    const int kind = !jp.sum.tiles ? kDenseBits : (jp.aggregate ? kDenseSumCount : kDenseSumProject);
+    const bool bits = kind == kDenseBits;
     cudaStream_t st = c->stream;
     const int sm = c->sm_count;
     CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
@@ -324,34 +333,54 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in row binning (flags %u)", c->h_sc->err);
     const uint64_t n_heavy = c->h_sc->nrows[3] + c->h_sc->nrows[4];
     const uint64_t cd_all = c->h_sc->outj_cls[3] + c->h_sc->outj_cls[4];
+    skip = 2;  // no heavy rows, or too little heavy work
     if (n_heavy == 0 || cd_all == 0) return DIM3G_OK;
     if (mode == 1 && cd_all < kDenseMinCand) return DIM3G_OK;
+    skip = 3;  // the budget holds no row or no K
     const uint64_t Np = round_up(m, kDenseBN), Wd = Np / 32;
-    // rows the bitmap budget holds, whole 128-row tiles
-    const uint64_t fit = c->prm.dense_mem / (Wd * 4) / kDenseBM * kDenseBM;
+    // bitmap: the rows its budget holds, whole 128-row tiles; summaries keep
+    // no bitmap and take every heavy row (their operand counts are bounded
+    // by the same budget through K below)
+    const uint64_t fit = bits ? c->prm.dense_mem / (Wd * 4) / kDenseBM * kDenseBM : n_heavy;
     const uint64_t nd = n_heavy < fit ? n_heavy : fit;
     if (nd == 0) return DIM3G_OK;
-    const uint64_t Mp = round_up(nd, kDenseBM), dbytes = Mp * Wd * 4;
+    const uint64_t Mp = round_up(nd, kDenseBM), dbytes = bits ? Mp * Wd * 4 : 0;
+    uint64_t kmax = c->prm.dense_k_max;
+    if (!bits) {
+        const uint64_t kfit = c->prm.dense_mem / ((Mp + Np) * 4) / kDenseBK * kDenseBK;  // 32-bit counts
+        if (kfit < kmax) kmax = kfit;
+        if (kmax == 0) return DIM3G_OK;
+    }
     const double t_bitmap = 3.0 * (double)dbytes / kDenseBw;
-    const double tiles_per_sm = ceil((double)(Mp / kDenseBM) * (double)(Np / kDenseBN) / sm);
-    auto t_product = [&](uint64_t Kp) {
+    const double ntile_all = (double)(Mp / kDenseBM) * (double)(Np / kDenseBN);
+    const double tiles_per_sm = ceil(ntile_all / sm);
+    const double tile_fixed = bits ? kDenseTileS : kDenseTileSumS;
+    auto t_product = [&](uint64_t Kp, double light) {
         const double t_mma = 2.0 * kDenseBM * kDenseBN * (double)Kp / kDenseSmFlops;
-        return tiles_per_sm * (t_mma > kDenseTileS ? t_mma : kDenseTileS);
+        // summaries also count the operands in 32 bits first, and every
+        // epilogue thread scans its tile's light bucket
+        const double t_ops = bits ? 0.0 : (double)(Mp + Np) * Kp * 9.0 / kDenseBw;
+        const double t_epi = tile_fixed + (bits ? 0.0 : kDenseBucketS * light / ntile_all);
+        return tiles_per_sm * (t_mma > t_epi ? t_mma : t_epi) + t_ops;
     };
-    const double t_min = t_product(kDenseBK) + t_bitmap;
+    // light candidates: OR-ed into the bitmap, or counted and bucketed by tile
+    const double light_bytes = bits ? kLightBytes : 2.0 * kLightBytes;
+    const double t_min = t_product(kDenseBK, 0.0) + t_bitmap;
     // the sparse cost of all heavy rows bounds that of any prefix of them
+    skip = 4;  // the cost model keeps the sparse path
     if (mode == 1 && t_min >= (double)cd_all * 4.0 / kSparseBw) return DIM3G_OK;
 
     CU(cudaEventRecord(c->evd[0], st));
     uint32_t* degd = ws_get<uint32_t>(c, k);
     int32_t* hid = ws_get<int32_t>(c, k);
-    uint32_t* hy = ws_get<uint32_t>(c, c->prm.dense_k_max);
-    unsigned int* bin_n = ws_get<unsigned int>(c, kDenseBins + 1);  // [kDenseBins]: heavy-column counter
-    unsigned long long* bin_mass = ws_get<unsigned long long>(c, kDenseBins);
+    uint32_t* hy = ws_get<uint32_t>(c, kmax);
+    // bin_n[kDenseBins]: heavy-column counter, [+1]: multiplicity flag, [+2]: largest light bucket
+    unsigned int* bin_n = ws_get<unsigned int>(c, kDenseBins + 3);
+    unsigned long long* bin_mass = ws_get<unsigned long long>(c, kDenseBins + 1);  // [kDenseBins]: light total
     if (!degd || !hid || !hy || !bin_n || !bin_mass) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense)");
     CU(cudaMemsetAsync(degd, 0, (size_t)k * 4, st));
-    CU(cudaMemsetAsync(bin_n, 0, (kDenseBins + 1) * 4, st));
-    CU(cudaMemsetAsync(bin_mass, 0, kDenseBins * 8, st));
+    CU(cudaMemsetAsync(bin_n, 0, (kDenseBins + 3) * 4, st));
+    CU(cudaMemsetAsync(bin_mass, 0, (kDenseBins + 1) * 8, st));
     // a sample of about 8192 heavy rows estimates the join values' mass
     const uint32_t step = nd > 8192 ? (uint32_t)(nd / 8192) : 1u;
     k_dense_deg<<<grid_for((nd / step + 1) * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, step, degd);
@@ -369,20 +398,23 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     for (uint32_t b = 0; b < kDenseBins; b++) sampled += (double)hm[b] * step;
     const double cd = nd < n_heavy ? sampled : (double)cd_all;
     const double t_sparse = cd * 4.0 / kSparseBw;
-    // the heavy join values: whole bins from the top, at most dense_k_max
-    // of them; the cut with the lowest modelled cost (mode 2: the most)
+    // the heavy join values: whole bins from the top, at most kmax of them;
+    // the cut with the lowest modelled cost (mode 2: the most)
     uint64_t kc = 0, best_k = 0;
     double heavy = 0;
     uint32_t best_cut = kDenseBins;
     double best_t = 0, best_light = 0;
     for (int b = (int)kDenseBins - 1; b >= 0; b--) {
         if (!hn[b]) continue;
-        if (kc + hn[b] > c->prm.dense_k_max) break;
+        if (kc + hn[b] > kmax) break;
         kc += hn[b];
         heavy += (double)hm[b] * step;
         const uint64_t Kp = round_up(kc, kDenseBK);
         const double light = sampled > heavy ? sampled - heavy : 0.0;
-        const double t = t_product(Kp) + t_bitmap + light * kLightBytes / kDenseBw;
+        const double t = t_product(Kp, light) + t_bitmap + light * light_bytes / kDenseBw;
+        // summaries: each epilogue thread scans its tile's light bucket, so
+        // only cuts with a small average bucket qualify
+        if (!bits && light > (double)ntile_all * kDenseBucketMax / 4 && b > 0) continue;
         if (mode == 2 || best_k == 0 || t < best_t) {
             best_t = t;
             best_k = kc;
@@ -393,49 +425,111 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     if (best_k == 0) return DIM3G_OK;
     if (mode == 1 && best_t >= t_sparse) return DIM3G_OK;
     const uint32_t Kp = (uint32_t)round_up(best_k, kDenseBK);
+    const uint32_t mt = (uint32_t)(Mp / kDenseBM), nt = (uint32_t)(Np / kDenseBN);
+    const uint64_t ntile = (uint64_t)mt * nt;
     uint8_t* A = ws_get<uint8_t>(c, Mp * Kp);
     uint8_t* B = ws_get<uint8_t>(c, Np * Kp);
-    uint32_t* D = ws_get<uint32_t>(c, Mp * Wd);
-    if (!A || !B || !D) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense operands)");
+    uint32_t* D = bits ? ws_get<uint32_t>(c, Mp * Wd) : nullptr;
+    if (!A || !B || (bits && !D)) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense operands)");
     k_dense_hid<<<grid_for(k, sm), 256, 0, st>>>(degd, rc.JR_S, rc.T, k, best_cut, hid, hy, bin_n + kDenseBins);
     CHECK_LAUNCH();
-    CU(cudaMemsetAsync(A, 0, Mp * Kp, st));
-    CU(cudaMemsetAsync(B, 0, Np * Kp, st));
-    k_dense_fill_a<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, hid, A, Kp);
-    CHECK_LAUNCH();
-    k_dense_fill_b<<<dim3(16, (unsigned)best_k), 256, 0, st>>>(rc.JR_S, rc.IC_S, rc.T, hy, B, Kp);
-    CHECK_LAUNCH();
+    DenseSum ds{};
+    if (bits) {
+        CU(cudaMemsetAsync(A, 0, Mp * Kp, st));
+        CU(cudaMemsetAsync(B, 0, Np * Kp, st));
+        k_dense_fill_a<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, hid, A, Kp);
+        CHECK_LAUNCH();
+        k_dense_fill_b<<<dim3(16, (unsigned)best_k), 256, 0, st>>>(rc.JR_S, rc.IC_S, rc.T, hy, B, Kp);
+        CHECK_LAUNCH();
+    } else {
+        // multiplicities, then e4m3 codes (a multiplicity above 16 keeps the
+        // sparse path); the light candidates bucketed by product tile
+        uint32_t* A32 = ws_get<uint32_t>(c, Mp * Kp);
+        uint32_t* B32 = ws_get<uint32_t>(c, Np * Kp);
+        uint32_t* tcnt = ws_get<uint32_t>(c, ntile + 1);
+        uint32_t* toff = ws_get<uint32_t>(c, ntile + 1);
+        uint32_t* tcur = ws_get<uint32_t>(c, ntile + 1);
+        uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(ntile + 1));
+        if (!A32 || !B32 || !tcnt || !toff || !tcur || !bsum)
+            return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense counts)");
+        unsigned int* flag = bin_n + kDenseBins + 1;
+        unsigned long long* ltotal = bin_mass + kDenseBins;
+        CU(cudaMemsetAsync(A32, 0, Mp * Kp * 4, st));
+        CU(cudaMemsetAsync(B32, 0, Np * Kp * 4, st));
+        CU(cudaMemsetAsync(tcnt, 0, (ntile + 1) * 4, st));
+        k_dense_cnt_a<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, list_m, (uint32_t)nd, hid, A32, Kp);
+        CHECK_LAUNCH();
+        k_dense_cnt_b<<<dim3(16, (unsigned)best_k), 256, 0, st>>>(rc.JR_S, rc.IC_S, rc.T, hy, B32, Kp);
+        CHECK_LAUNCH();
+        k_dense_to_fp8<<<grid_for(Mp * Kp, sm), 256, 0, st>>>(A32, A, Mp * Kp, flag);
+        CHECK_LAUNCH();
+        k_dense_to_fp8<<<grid_for(Np * Kp, sm), 256, 0, st>>>(B32, B, Np * Kp, flag);
+        CHECK_LAUNCH();
+        k_dense_light<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, rc.JR_S, rc.IC_S, rc.T, list_m,
+                                                             (uint32_t)nd, hid, LightCount{tcnt, nt});
+        CHECK_LAUNCH();
+        k_dense_maxcnt<<<grid_for(ntile, sm), 256, 0, st>>>(tcnt, ntile, flag + 1);
+        CHECK_LAUNCH();
+        SCAN(U32Src{tcnt}, RowPtrDst{toff, tcur}, ntile + 1, bsum, ltotal);
+        unsigned int hflag[2] = {0, 0};
+        unsigned long long hl = 0;
+        CU(cudaMemcpyAsync(hflag, flag, 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(&hl, ltotal, 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        // not exact in e4m3, or light buckets too large for the epilogue
+        c->stats.dense_bucket_max = hflag[1];
+        skip = hflag[0] ? 5 : 6;
+        if (hflag[0] || hflag[1] > kDenseBucketMax || hl >= 0xFFFFFFFFull) return DIM3G_OK;
+        uint16_t* lb = ws_get<uint16_t>(c, hl + 1);
+        if (!lb) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense light buckets)");
+        k_dense_light<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, rc.JR_S, rc.IC_S, rc.T, list_m,
+                                                             (uint32_t)nd, hid, LightScatter{tcur, lb, nt});
+        CHECK_LAUNCH();
+        ds = DenseSum{list_m, (uint32_t)nd, rc.id2x, rc.id2z, toff, lb, jp.sum};
+        best_light = (double)hl;
+    }
     CUtensorMap mA, mB;
     int r = dense_map(c, &mA, A, Mp, Kp, kDenseBM);
     if (!r) r = dense_map(c, &mB, B, Np, Kp, kDenseBN);
     if (r) return r;
-    const uint32_t mt = (uint32_t)(Mp / kDenseBM), nt = (uint32_t)(Np / kDenseBN);
-    const uint64_t ntile = (uint64_t)mt * nt;
+    const unsigned grid = (unsigned)(ntile < (uint64_t)sm ? ntile : (uint64_t)sm);
     CU(cudaEventRecord(c->evd[1], st));
-    k_dense_mma<<<(unsigned)(ntile < (uint64_t)sm ? ntile : (uint64_t)sm), kDenseThreads, kDenseSmem, st>>>(
-        mA, mB, D, (uint32_t)Wd, mt, nt, Kp / kDenseBK, &sc->err);
+    if (kind == kDenseBits)
+        k_dense_mma<kDenseBits><<<grid, kDenseThreads, kDenseSmem, st>>>(mA, mB, D, (uint32_t)Wd, mt, nt, Kp / kDenseBK,
+                                                                          &sc->err, ds);
+    else if (kind == kDenseSumProject)
+        k_dense_mma<kDenseSumProject><<<grid, kDenseSumThreads, kDenseSmem, st>>>(mA, mB, nullptr, 0, mt, nt,
+                                                                                   Kp / kDenseBK, &sc->err, ds);
+    else
+        k_dense_mma<kDenseSumCount><<<grid, kDenseSumThreads, kDenseSmem, st>>>(mA, mB, nullptr, 0, mt, nt,
+                                                                                 Kp / kDenseBK, &sc->err, ds);
     CHECK_LAUNCH();
     CU(cudaEventRecord(c->evd[2], st));
-    k_dense_light<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, rc.JR_S, rc.IC_S, rc.T, list_m,
-                                                         (uint32_t)nd, hid, D, (uint32_t)Wd);
-    CHECK_LAUNCH();
-    // chunk popcounts and their offsets
-    const uint32_t cpr = (uint32_t)((Wd + 31) / 32);
-    const uint64_t nc = nd * cpr;
-    uint32_t* cc = ws_get<uint32_t>(c, nc + 1);
-    unsigned long long* coff = ws_get<unsigned long long>(c, nc + 1);
-    uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(nc + 1));
-    if (!cc || !coff || !bsum) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense chunks)");
-    k_dense_chunks<<<grid_for(nc * 8, sm), 256, 0, st>>>((uint32_t)nd, D, (uint32_t)Wd, cpr, cc);
-    CHECK_LAUNCH();
-    SCAN(U32Src{cc}, OffDst{coff}, nc + 1, bsum, nullptr);
+    uint32_t cpr = 0;
+    unsigned long long* coff = nullptr;
+    if (bits) {
+        k_dense_light<<<grid_for(nd * 32, sm), 256, 0, st>>>(rc.JR_R, rc.IC_R, rc.JR_S, rc.IC_S, rc.T, list_m,
+                                                             (uint32_t)nd, hid, LightOr{D, (uint32_t)Wd});
+        CHECK_LAUNCH();
+        // chunk popcounts and their offsets
+        cpr = (uint32_t)((Wd + 31) / 32);
+        const uint64_t nc = nd * cpr;
+        uint32_t* cc = ws_get<uint32_t>(c, nc + 1);
+        coff = ws_get<unsigned long long>(c, nc + 1);
+        uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(nc + 1));
+        if (!cc || !coff || !bsum) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (dense chunks)");
+        k_dense_chunks<<<grid_for(nc * 8, sm), 256, 0, st>>>((uint32_t)nd, D, (uint32_t)Wd, cpr, cc);
+        CHECK_LAUNCH();
+        SCAN(U32Src{cc}, OffDst{coff}, nc + 1, bsum, nullptr);
+    }
     CU(cudaEventRecord(c->evd[3], st));
     {
-        // the bitmap-class kernels take the rows after the block's
+        // the row-class kernels take the heavy rows after the block's
         const unsigned long long rest[2] = {n_heavy - nd, 0};
         CU(cudaMemcpyAsync(&sc->nrows[3], rest, sizeof rest, cudaMemcpyHostToDevice, st));
         CU(cudaStreamSynchronize(st));  // `rest` is on this frame
     }
+    skip = 0;
     c->stats.rows_dense = (uint32_t)nd;
     c->stats.heavy_y = (uint32_t)best_k;
     c->stats.dense_kp = Kp;
@@ -639,6 +733,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CU(cudaEventRecord(c->ev[3], st));
         CU(cudaStreamSynchronize(st));
         if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in summary (flags %u)", c->h_sc->err);
+        dense_times(c, dp);
         S.out_j = c->h_sc->outj;
         S.rows_warp = (uint32_t)c->h_sc->nrows[1];
         S.rows_block = (uint32_t)c->h_sc->nrows[2];
@@ -1039,8 +1134,12 @@ int dim3g_create(int device, dim3g_ctx** out) {
                                    ((1 << 14) + 32 * (int)kStage) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
-              cudaFuncSetAttribute(k_dense_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseSmem) ==
-                  cudaSuccess &&
+              cudaFuncSetAttribute(k_dense_mma<kDenseBits>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kDenseSmem) == cudaSuccess &&
+              cudaFuncSetAttribute(k_dense_mma<kDenseSumProject>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kDenseSmem) == cudaSuccess &&
+              cudaFuncSetAttribute(k_dense_mma<kDenseSumCount>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kDenseSmem) == cudaSuccess &&
               cudaFuncSetAttribute(k_dense_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDenseEmitSmem) ==
                   cudaSuccess &&
               set_aggregate_attributes();

@@ -47,7 +47,7 @@ class Stats(ctypes.Structure):
         ("ms_count_cls", ctypes.c_float * 3), ("ms_write_cls", ctypes.c_float * 3),
         ("out_j_cls", ctypes.c_uint64 * 3), ("n_out_cls", ctypes.c_uint64 * 3),
         ("ms_dense", ctypes.c_float * 3), ("dense_kp", ctypes.c_uint32),
-        ("dense_light", ctypes.c_uint64),
+        ("dense_light", ctypes.c_uint64), ("dense_skip", ctypes.c_uint32), ("dense_bucket_max", ctypes.c_uint32),
     ]
 
     def as_dict(self):

@@ -95,3 +95,43 @@ def test_dense_block_off_and_knobs(ctx):
     ctx.set_param("dense_block", 0)
     assert ctx.get_param("dense_block") == 0
     ctx.set_param("dense_block", 1)
+
+
+@pytest.mark.timeout(600, method="thread")
+@pytest.mark.parametrize("kmax", [32, 4096])
+def test_dense_block_summaries_match_oracle(built, golden, kmax):
+    """Per-A-tile summaries with the dense block forced: the product's
+    counts in the fused epilogue, the light candidates bucketed by tile and
+    added per group, equal the oracle's tile summaries of the join-project
+    and the COUNT join-aggregate, on all tiles and on a slice.  With few
+    join values in the product most candidates are light and the buckets
+    too large, so the sparse kernels run instead (exact either way)."""
+    import torch
+    from oracle import oracle_py as O
+    index, arrays = golden
+    c = _ctx({"dense_block": 2, "dense_k_max": kmax, "warp_slots_log2": 5, "block_slots_log2": 8})
+    used = []
+    for name in ["grd_small", "grd_swap", "grd_dense_z", "heavy_duplicates", "one_join_value", "zipf_1m_s001",
+                 "chung_lu_s0005", "chung_lu_s005"]:
+        R, S = case_inputs(name, index, arrays)
+        dR, dS = _dev(R), _dev(S)
+        wp, n, _, _ = O.join_project(R, S)
+        wg, wc, ng, _, _ = O.join_count(R, S)
+        tiles = 64
+        want_p = O.tile_summary(wp.reshape(-1, 2) if n else np.empty((0, 2), np.uint32), None, tiles)
+        want_c = O.tile_summary(wg.reshape(-1, 2) if ng else np.empty((0, 2), np.uint32),
+                                wc if ng else np.empty(0, np.uint64), tiles)
+        got_p = c.join_project_summary(dR, R.shape[0], dS, S.shape[0], tiles)
+        used_p = c.stats()["rows_dense"]
+        got_c = c.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles)
+        used_c = c.stats()["rows_dense"]
+        assert np.array_equal(got_p, want_p), name
+        assert np.array_equal(got_c, want_c), name
+        lo, hi = 8, 24
+        sl = c.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles, lo, hi)
+        assert np.array_equal(sl[lo:hi], want_c[lo:hi]) and not sl[:lo].any() and not sl[hi:].any(), name
+        if used_p and used_c:
+            used.append(name)
+    if kmax == 4096:
+        assert len(used) >= 3, used
+    c.close()
