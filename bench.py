@@ -432,7 +432,7 @@ def run_count16m(args, rank, world, local_rank):
     for k in range(args.warmup):
         ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles, k % tiles, k % tiles + 1)
     launches0 = ctx.stats()["launches"]
-    groups, outj, ms_dev = 0, 0, 0.0
+    groups, outj, ms_dev, ms_mma, flops = 0, 0, 0.0, 0.0, 0
     with ClockSampler(local_rank) as clk:
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -441,7 +441,11 @@ def run_count16m(args, rank, world, local_rank):
             sm = ctx.join_count_summary(dR, R.shape[0], dS, S.shape[0], tiles, k % tiles, k % tiles + 1)
             groups += int(sm[:, 0].sum())
             outj += int(sm[:, 1].sum())
-            ms_dev += ctx.stats()["ms_write"]
+            st = ctx.stats()
+            ms_dev += st["ms_write"]
+            if st["rows_dense"]:
+                ms_mma += st["ms_dense"][1]
+                flops += 2 * ((st["rows_dense"] + 127) // 128 * 128) * ((st["nz"] + 255) // 256 * 256) * st["dense_kp"]
         ev1.record(stream)
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1) / args.steps
@@ -459,6 +463,20 @@ def run_count16m(args, rank, world, local_rank):
                "kind": "port", "sample": "1/4096 A-slice of count16m (full S): %d groups in %.2f s" % (ng, dt)}
     # expansion of the slices: 4 B per candidate read, nothing written
     alg = 4 * outj
+    if flops:
+        # the dense block ran: its product (fp8 MMA, exact counts) with the
+        # group-hash epilogue is the dominant kernel
+        ach = flops / (ms_mma / 1e3) / 1e12
+        roof = {"bound": "tensor", "kernel": "k_dense_mma (COUNT summary epilogue)", "achieved": round(ach, 1),
+                "peak": 4500.0, "peak_kind": "nominal fp8 dense (the measured peaks are bf16 only)",
+                "unit": "TFLOP/s", "frac": round(ach / 4500.0, 4), "traffic": None,
+                "flops_per_launch": int(flops / max(args.steps, 1)), "ms_per_launch": round(ms_mma / args.steps, 3),
+                "kp": st["dense_kp"], "note": "the epilogue's two splitmix64 hashes per group bound the tile rate"}
+    else:
+        roof = {"bound": "hbm", "kernel": "k_agg_tile (summaries)",
+                "achieved": round(alg / (ms_dev / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": round(alg / (ms_dev / 1e3) / 1e9 / peak, 4), "traffic": None,
+                "alg_bytes_per_launch": int(alg / max(args.steps, 1))}
     line = {
         "metric": "distinct (a,c) groups Mgroups/s, COUNT(*) GROUP BY (A,C) 16M x 16M Zipf 1.2",
         "value": round(groups / (ms * args.steps / 1e3) / 1e6, 3), "unit": "Mgroups/s", "n_gpus": world,
@@ -466,10 +484,7 @@ def run_count16m(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64", "data": "synthetic",
         "config": {"workload": "count16m", "desc": WORKLOADS["count16m"], "groups": groups, "out_j": outj,
                    "slices": args.steps, "l2": "relations > L2; no flush"},
-        "roofline": {"bound": "hbm", "kernel": "k_agg_tile (summaries)",
-                     "achieved": round(alg / (ms_dev / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
-                     "unit": "GB/s", "frac": round(alg / (ms_dev / 1e3) / 1e9 / peak, 4), "traffic": None,
-                     "alg_bytes_per_launch": int(alg / max(args.steps, 1))},
+        "roofline": roof,
         "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": None,
     }
     if rank == 0:
