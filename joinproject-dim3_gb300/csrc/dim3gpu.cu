@@ -347,7 +347,11 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     const uint64_t Mp = round_up(nd, kDenseBM), dbytes = bits ? Mp * Wd * 4 : 0;
     uint64_t kmax = c->prm.dense_k_max;
     if (!bits) {
-        const uint64_t kfit = c->prm.dense_mem / ((Mp + Np) * 4) / kDenseBK * kDenseBK;  // 32-bit counts
+        // the product's tiles are indexed in 32 bits; their light-bucket
+        // bounds take 12 B each out of the budget
+        const uint64_t tiles = (Mp / kDenseBM) * (Np / kDenseBN);
+        if (tiles >= (1ull << 31) || tiles * 12 >= c->prm.dense_mem) return DIM3G_OK;
+        const uint64_t kfit = (c->prm.dense_mem - tiles * 12) / ((Mp + Np) * 4) / kDenseBK * kDenseBK;  // 32-bit counts
         if (kfit < kmax) kmax = kfit;
         if (kmax == 0) return DIM3G_OK;
     }
