@@ -4,23 +4,32 @@
 //
 // Here the heavy rows X_d (the bitmap classes) are joined through the K join
 // values y with the largest candidate mass deg_Xd(y) * deg_S(y) as one
-// boolean matrix product on tcgen05:
-//   A (|X_d| x K)  A[i][h] = 1 when R row x_i holds y_h      (fp8 e4m3 1.0)
-//   B (m x K)      B[z][h] = 1 when S holds (z, y_h)
-//   C = A * B^T    fp32 accumulators in TMEM, exact integers (< 2^24)
-// and the epilogue keeps one bit per (x_i, z): C > 0.  The bits form a
-// row-major bitmap D (|X_d| x m).  The remaining (light) join values of the
-// heavy rows are expanded into the same bitmap with atomicOr, and the rows'
-// pairs are emitted from it.  The result is exactly the rows' distinct z
-// sets: a bit is set iff some y joins x and z.
+// matrix product on tcgen05:
+//   A (|X_d| x K)  A[i][h] = multiplicity of (x_i, y_h) in R   (fp8 e4m3)
+//   B (m x K)      B[z][h] = multiplicity of (z, y_h) in S
+//   C = A * B^T    f32 accumulators in TMEM: the number of join tuples of
+//                  (x_i, z) through the K values, exact: multiplicities are
+//                  at most 16 (exact in e4m3) and K at most 4096, so
+//                  C <= 16 * 16 * 4096 = 2^20 < 2^24
+// (the join-project writes 1.0 for any multiplicity; only C > 0 matters).
+// The other (light) join values of the heavy rows go through a sparse pass.
+//   join-project: the epilogue keeps one bit per (x_i, z), C > 0, in a
+//     row-major bitmap D (|X_d| x m); the light candidates are OR-ed in and
+//     the rows' pairs are emitted from it.
+//   per-A-tile summaries: the light candidates are bucketed by product tile
+//     and the epilogue adds them to C group by group, summing groups,
+//     counts and group hashes per A-tile; nothing is materialised.
+// Either way the result is exact: a bit or a group exists iff some y joins
+// x and z, and a group's count is its number of join tuples.
 //
 // The product is a persistent kernel, one CTA per SM: warp 0 loads A and B
 // tiles with TMA (128-byte swizzle) through a 4-stage shared-memory ring,
 // warp 1 issues the MMAs (one thread; 128 x 256 x 32 per instruction) into
-// one of two TMEM accumulators, and warps 2-5 read the other accumulator
-// (tcgen05.ld), threshold and store the bits.  Every wait on an mbarrier is
-// bounded by time; a wait that runs out sets kErrDenseTimeout, stops the
-// CTA's loops, and the CTA still frees its TMEM before it exits.
+// one of two TMEM accumulators, and the epilogue warps (8 for the bitmap,
+// 16 for summaries) read the other accumulator (tcgen05.ld).  Every wait on
+// an mbarrier is bounded by time; a wait that runs out sets
+// kErrDenseTimeout, stops the CTA's loops, and the CTA still frees its TMEM
+// before it exits.
 #pragma once
 #include <cuda.h>
 
