@@ -736,4 +736,7 @@ def workload(name, scale=1.0):
     if name == "gen_rand_data":
         n = max(1, int(10 ** 7 * scale))
         return gen_rand_data(n, n, 10 ** 6, 10 ** 6, 10 ** 6, 492)
+    if name == "grd_all_dense":  # 3000 x 100 x 3000 domains: every (x, z) group exists
+        n = max(1, int(300000 * scale))
+        return gen_rand_data(n, n, 3000, 100, 3000, 492)
     raise KeyError(name)
