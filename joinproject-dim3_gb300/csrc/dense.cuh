@@ -280,6 +280,28 @@ struct DenseSum {
     SumAcc sum;
 };
 
+// pair_hash(a, c) = splitmix64 finaliser of a << 32 | c, with the terms
+// that depend on the row's a alone hoisted out: after the first shift-xor
+// the high word is a ^ (a >> 30) and the low word c ^ (a << 2) ^ (c >> 30),
+// and the high word's share of the first product is a constant shifted
+// into the high half.  Equal to pair_hash for every a, c.
+struct PairRow {
+    uint32_t a2;             // a << 2
+    unsigned long long k1;   // ((a ^ (a >> 30)) * low word of the multiplier) << 32
+};
+__device__ __forceinline__ PairRow pair_row(uint32_t a) {
+    return PairRow{a << 2, (unsigned long long)((a ^ (a >> 30)) * 0x1ce4e5b9u) << 32};
+}
+__device__ __forceinline__ unsigned long long pair_hash_row(const PairRow& r, uint32_t c) {
+    unsigned long long v = (unsigned long long)(c ^ r.a2 ^ (c >> 30)) * 0xbf58476d1ce4e5b9ull + r.k1;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebull;
+    return v ^ (v >> 31);
+}
+// An exact f32 integer below 2^23 as an integer: one add, no conversion.
+__device__ __forceinline__ uint32_t count_of(uint32_t fbits) {
+    return __float_as_uint(__uint_as_float(fbits) + 8388608.0f) - 0x4B000000u;
+}
+
 // Adds a group's summary terms; light corrections replace a group's count.
 template <int kMode>
 __device__ __forceinline__ void dense_group(uint32_t a, uint32_t c, uint32_t cnt, unsigned long long& g,
@@ -298,7 +320,8 @@ __device__ __forceinline__ void dense_group(uint32_t a, uint32_t c, uint32_t cnt
 // then the tile's light candidates of this row and chunk (each distinct
 // (row, z) once, with the number of its entries as its light count).
 template <int kMode>
-__device__ __forceinline__ void dense_sum_chunk(const uint32_t (&v)[32], const DenseSum& ds, uint32_t a, uint32_t z0,
+__device__ __forceinline__ void dense_sum_chunk(const uint32_t (&v)[32], const DenseSum& ds, uint32_t a,
+                                                const PairRow& pr, uint32_t z0,
                                                 uint32_t key0, uint32_t l0, uint32_t l1, unsigned long long& g,
                                                 unsigned long long& cs, unsigned long long& h) {
     // branch-free over the 32 columns so their hash chains interleave; the
@@ -309,10 +332,10 @@ __device__ __forceinline__ void dense_sum_chunk(const uint32_t (&v)[32], const D
         const uint32_t zq[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
         for (uint32_t r = 0; r < 4; r++) {
-            const uint32_t cnt = (uint32_t)__uint_as_float(v[4 * q + r]);
+            const uint32_t cnt = count_of(v[4 * q + r]);
             const bool p = cnt != 0;
-            const unsigned long long hv =
-                kMode == kDenseSumCount ? group_hash(a, zq[r], cnt) : pair_hash(a, zq[r]);
+            const unsigned long long ph = pair_hash_row(pr, zq[r]);
+            const unsigned long long hv = kMode == kDenseSumCount ? mix64(ph + cnt) : ph;
             h += p ? hv : 0ull;
             g += p;
             cs += kMode == kDenseSumCount ? cnt : (uint32_t)p;
@@ -486,6 +509,7 @@ static __global__ void __launch_bounds__(kMode == kDenseBits ? kDenseThreads : k
         uint32_t tb = 0, tph = 0;
         // summary state: this lane's row (block row cur_mi * 128 + row)
         uint32_t cur_mi = ~0u, a = 0, stile = 0;
+        PairRow pr{0, 0};
         bool live = false;
         unsigned long long g = 0, cs = 0, h = 0;
         for (uint32_t t = blockIdx.x; t < ntile && !bad; t += gridDim.x) {
@@ -506,6 +530,7 @@ static __global__ void __launch_bounds__(kMode == kDenseBits ? kDenseThreads : k
                 if (nlive) stile = ntl;
                 cur_mi = mi;
                 a = na;
+                pr = pair_row(na);
                 live = nlive;
             }
             // warp-uniform outcome: the TMEM loads below are warp-collective
@@ -526,7 +551,7 @@ static __global__ void __launch_bounds__(kMode == kDenseBits ? kDenseThreads : k
                         mbar_arrive(tempty + 8 * tb);  // the accumulator is in registers
                     }
                     if (live)
-                        dense_sum_chunk<kMode>(v, ds, a, ni * kDenseBN + hc * pcols + j * 32,
+                        dense_sum_chunk<kMode>(v, ds, a, pr, ni * kDenseBN + hc * pcols + j * 32,
                                                (row << 8) | (hc * pcols + j * 32), l0, l1, g, cs, h);
                 }
                 if (++tb == 2) {
