@@ -90,7 +90,11 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * 1 when the cost model prefers it, 2 whenever its bitmap fits),
  * "dense_k_max" (32..4096: most join values in that product),
  * "dense_mem_mb" (bitmap budget of that product, default 16384: it takes as
- * many heavy rows as their x z bitmap fits, the largest first). */
+ * many heavy rows as their x z bitmap fits, the largest first),
+ * "keep_roles" (0: the larger relation drives the join, the reference's
+ * swap at dim3.hpp:993-994, so a smaller R yields (S.first, R.first) pairs;
+ * 1: R always drives and pairs are always (R.first, S.first) -- for joining
+ * an A-slice of R with all of S, which keeps the whole join's row shape). */
 int dim3g_set_param(dim3g_ctx* ctx, const char* name, int64_t value);
 int dim3g_get_param(const dim3g_ctx* ctx, const char* name, int64_t* value);
 /* Release device memory cached by the context (workspace, staging). */
@@ -169,8 +173,11 @@ int dim3g_join_count_summary(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, c
  * current); make that first call before any stream capture.  All calls share
  * the array: calls that overlap on the GPU race, so serialise them.  The
  * result set, *n_out and DIM3G_ERR_CAPACITY are as for
- * dim3g_join_project_device.  cuda_stream is a cudaStream_t (NULL: the
- * default stream), synchronised before the call returns. */
+ * dim3g_join_project_device.  d_R, d_S and d_out must be 8-byte aligned
+ * (DIM3G_ERR_INVALID otherwise, before anything runs on the GPU).  An error
+ * already pending on the calling thread's CUDA state is reported as
+ * DIM3G_ERR_CUDA and left in place.  cuda_stream is a cudaStream_t (NULL:
+ * the default stream), synchronised before the call returns. */
 #define DIM3G_NOALLOC_MAX_TUPLES (1u << 18)
 #define DIM3G_NOALLOC_MAX_PAIRS (1u << 20)
 int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS,

@@ -84,6 +84,7 @@ struct Params {
     uint32_t dense = 1;       // dense block on the tensor cores: 0 off, 1 by cost model, 2 whenever it fits
     uint32_t dense_k_max = 2048;  // most join values in the dense product
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
+    bool keep_roles = false;  // R drives the join whatever the sizes (no swap)
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -1007,7 +1008,7 @@ int host_join(dim3g_ctx* c, const uint32_t* R, uint64_t nR, const uint32_t* S, u
     if (out_alloc) *out_alloc = nullptr;
     if (cnt_alloc) *cnt_alloc = nullptr;
     CU(cudaSetDevice(c->device));
-    const bool swap = nR < nS;
+    const bool swap = !c->prm.keep_roles && nR < nS;
     const uint32_t* P = swap ? S : R;
     const uint32_t* Q = swap ? R : S;
     const uint64_t nP = swap ? nS : nR, nQ = swap ? nR : nS;
@@ -1224,6 +1225,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "dense_mem_mb")) {
         if (v < 1 || v > (1 << 20)) return fail(c, DIM3G_ERR_INVALID, "dense_mem_mb must be in 1..2^20");
         c->prm.dense_mem = (uint64_t)v << 20;
+    } else if (!strcmp(name, "keep_roles")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "keep_roles must be 0 or 1");
+        c->prm.keep_roles = v == 1;
     } else {
         return fail(c, DIM3G_ERR_INVALID, "unknown parameter %s", name);
     }
@@ -1242,6 +1246,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "dense_block")) *v = c->prm.dense;
     else if (!strcmp(name, "dense_k_max")) *v = c->prm.dense_k_max;
     else if (!strcmp(name, "dense_mem_mb")) *v = (int64_t)(c->prm.dense_mem >> 20);
+    else if (!strcmp(name, "keep_roles")) *v = c->prm.keep_roles ? 1 : 0;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }
@@ -1277,7 +1282,7 @@ int dim3g_join_project_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, con
         return fail(c, DIM3G_ERR_INVALID, "null argument");
     if (!aligned8(dR) || !aligned8(dS) || !aligned8(d_out)) return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
     CU(cudaSetDevice(c->device));
-    const bool swap = nR < nS;
+    const bool swap = !c->prm.keep_roles && nR < nS;
     DeviceOut d{(uint2*)d_out, nullptr, capacity};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
                 swap, false, false, !c->prm.ordered, OutPrep{prep_device, peek_device, &d}};
@@ -1289,7 +1294,7 @@ int dim3g_join_project_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t n
     if (!c || !n_out || (nR && !dR) || (nS && !dS)) return fail(c, DIM3G_ERR_INVALID, "null argument");
     if (!aligned8(dR) || !aligned8(dS)) return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
     CU(cudaSetDevice(c->device));
-    const bool swap = nR < nS;
+    const bool swap = !c->prm.keep_roles && nR < nS;
     DeviceOut d{nullptr, nullptr, 0};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
                 swap, false, true, false, OutPrep{prep_device, peek_device, &d}};
@@ -1309,7 +1314,7 @@ int dim3g_join_count_device(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const
     if (!aligned8(dR) || !aligned8(dS) || !aligned8(d_out_xz) || !aligned8(d_out_cnt))
         return fail(c, DIM3G_ERR_INVALID, "device pointers must be 8-byte aligned");
     CU(cudaSetDevice(c->device));
-    const bool swap = nR < nS;
+    const bool swap = !c->prm.keep_roles && nR < nS;
     DeviceOut d{(uint2*)d_out_xz, (unsigned long long*)d_out_cnt, capacity};
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
                 swap, true, false, false, OutPrep{prep_device, peek_device, &d}};
@@ -1332,7 +1337,7 @@ int run_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* d
     int r = ensure_dev(c, &c->d_sum, &c->d_sum_bytes, (size_t)tiles * 24);
     if (r) return r;
     CU(cudaMemsetAsync(c->d_sum, 0, (size_t)tiles * 24, c->stream));
-    const bool swap = nR < nS;
+    const bool swap = !c->prm.keep_roles && nR < nS;
     JoinPlan jp{(const uint2*)(swap ? dS : dR), swap ? nS : nR, (const uint2*)(swap ? dR : dS), swap ? nR : nS,
                 swap, aggregate, false, false, OutPrep{nullptr, nullptr, nullptr}};
     jp.sum = SumAcc{(unsigned long long*)c->d_sum, tiles - 1, lo, hi};

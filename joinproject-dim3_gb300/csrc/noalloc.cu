@@ -46,8 +46,8 @@ constexpr size_t kScratchBytes = kOffCounters + 256;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// counters: [0] distinct pairs found, [1] flags (bit 0: pair limit reached,
-// bit 1: probe limit), [2] the all-ones pair seen
+// counters: [0] distinct pairs found, [1] flags (bit 1: a probe walked the
+// whole pair table), [2] the all-ones pair seen
 struct Scratch {
     uint32_t* head;
     uint32_t* next;
@@ -95,10 +95,13 @@ __device__ void insert_pair(Scratch s, uint2* out, unsigned long long cap, uint3
         unsigned long long cur = ((volatile unsigned long long*)s.pairs)[h];
         if (cur == key) return;
         if (cur == kEmptyPair) {
-            if (((volatile unsigned long long*)s.counters)[0] >= kMaxPairs) {
-                atomicOr(&s.counters[1], 1ull);
-                return;
-            }
+            // The limit is decided after the fact: the counter only counts
+            // pairs that were claimed, so once it is above the limit the
+            // result is known to be too large and no more pairs are claimed
+            // (the host reports it from the final count).  Threads that pass
+            // this test together overshoot by at most the threads in flight,
+            // which the table's 2x slot count absorbs.
+            if (((volatile unsigned long long*)s.counters)[0] > kMaxPairs) return;
             unsigned long long prev = atomicCAS(&s.pairs[h], kEmptyPair, key);
             if (prev == kEmptyPair) {
                 emit(s, out, cap, px, qc);
@@ -122,30 +125,41 @@ __global__ void k_na_probe(const uint2* __restrict__ P, const uint2* __restrict_
     }
 }
 
-// Per-device scratch address, resolved once with that device current.
+// Per-device scratch address and grid size, resolved once with that device
+// current.
 std::mutex g_setup_mutex;
 std::atomic<unsigned char*> g_base[64];
+int g_grid[64];
 
-int scratch_for_device(int dev, unsigned char** base) {
+int scratch_for_device(int dev, unsigned char** base, int* grid) {
     if (dev < 0 || dev >= 64) return DIM3G_ERR_UNSUPPORTED;
     unsigned char* p = g_base[dev].load(std::memory_order_acquire);
     if (!p) {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
         p = g_base[dev].load(std::memory_order_relaxed);
         if (!p) {
+            int sms = 0;
+            if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+                cudaGetLastError();
+                return DIM3G_ERR_CUDA;
+            }
             void* addr = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&addr, g_scratch);
             if (e != cudaSuccess || !addr) {
                 cudaGetLastError();
                 return DIM3G_ERR_CUDA;
             }
+            g_grid[dev] = 4 * sms;  // 4 CTAs of 256 threads per SM
             p = (unsigned char*)addr;
             g_base[dev].store(p, std::memory_order_release);
         }
     }
     *base = p;
+    *grid = g_grid[dev];
     return DIM3G_OK;
 }
+
+bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
 
 }  // namespace
 
@@ -153,20 +167,26 @@ extern "C" int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, cons
                                           uint32_t* d_out, uint64_t capacity, uint64_t* n_out, void* cuda_stream) {
     if (!n_out || (nR && !d_R) || (nS && !d_S) || (capacity && !d_out)) return DIM3G_ERR_INVALID;
     *n_out = 0;
+    // the kernels read and write pairs as 8-byte words
+    if (!aligned8(d_R) || !aligned8(d_S) || !aligned8(d_out)) return DIM3G_ERR_INVALID;
     // the larger relation drives the build, exactly the reference's swap
     const bool swap = nR < nS;
     const uint2* P = (const uint2*)(swap ? d_S : d_R);
     const uint2* Q = (const uint2*)(swap ? d_R : d_S);
     const uint64_t nP = swap ? nS : nR, nQ = swap ? nR : nS;
+    if (nP == 0 || nQ == 0) return DIM3G_OK;            // an empty input joins to nothing
     if (nP > kMaxTuples) return DIM3G_ERR_UNSUPPORTED;  // beyond the fixed scratch
-    if (nP == 0 || nQ == 0) return DIM3G_OK;
+    // An error the caller left pending (from earlier, unrelated work) is
+    // reported and left in place, not taken as this call's launch status.
+    if (cudaPeekAtLastError() != cudaSuccess) return DIM3G_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return DIM3G_ERR_CUDA;
     }
     unsigned char* base = nullptr;
-    int r = scratch_for_device(dev, &base);
+    int grid = 0;
+    int r = scratch_for_device(dev, &base, &grid);
     if (r) return r;
     Scratch s{(uint32_t*)(base + kOffHead), (uint32_t*)(base + kOffNext), (unsigned long long*)(base + kOffPairs),
               (unsigned long long*)(base + kOffCounters)};
@@ -179,7 +199,6 @@ extern "C" int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, cons
         cudaGetLastError();
         return DIM3G_ERR_CUDA;
     }
-    const unsigned grid = 4 * 152;
     k_na_build<<<grid, 256, 0, st>>>(P, (uint32_t)nP, s);
     k_na_probe<<<grid, 256, 0, st>>>(P, Q, (uint32_t)nQ, s, (uint2*)d_out, capacity);
     unsigned long long h[2] = {0, 0};
@@ -188,7 +207,7 @@ extern "C" int dim3g_join_project_noalloc(const uint32_t* d_R, uint64_t nR, cons
         cudaGetLastError();
         return DIM3G_ERR_CUDA;
     }
-    if (h[1] & 1ull) return DIM3G_ERR_UNSUPPORTED;  // more distinct pairs than DIM3G_NOALLOC_MAX_PAIRS
+    if (h[0] > kMaxPairs) return DIM3G_ERR_UNSUPPORTED;  // more distinct pairs than DIM3G_NOALLOC_MAX_PAIRS
     if (h[1] & 2ull) return DIM3G_ERR_DEVICE;
     *n_out = h[0];
     return h[0] > capacity ? DIM3G_ERR_CAPACITY : DIM3G_OK;

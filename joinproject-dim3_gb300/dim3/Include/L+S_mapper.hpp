@@ -5,9 +5,11 @@
 // insert(v, recorder) also records recorder[id] = v, find(v) returns the id or
 // -1, size(), clear() (drops keys, keeps the counter), reset_cnt(),
 // __set_cnt(v), cache_map_bucket_count().  Each single-key call is one GPU
-// round trip; insert_batch / find_batch give the same ids for a whole array
-// in one call (ids in first-occurrence order, as a loop of insert() would).
-// Keys are 32-bit; the hasher type is accepted for signature compatibility.
+// round trip (a launch and a synchronisation, microseconds): code that maps
+// many keys should call insert_batch / find_batch, which give the same ids
+// for a whole array in one call (ids in first-occurrence order, as a loop of
+// insert() would).  All mappers share the process's one GPU context.  Keys
+// are 32-bit; the hasher type is accepted for signature compatibility.
 #pragma once
 
 #include <cstdio>
@@ -15,7 +17,7 @@
 #include <functional>
 #include <vector>
 
-#include "../../../include/dim3gpu.h"
+#include "dim3g_context.hpp"
 
 template <typename T = int, typename H = std::hash<T>, typename _Tcounter = int>
 struct LS_mapper {
@@ -33,14 +35,10 @@ struct LS_mapper {
 
    public:
     LS_mapper(_Tcounter n, int /*shr_bits*/ = 0, int /*cache_n*/ = 16384) {
-        const char* d = getenv("DIM3G_DEVICE");
-        check(dim3g_create(d ? atoi(d) : 0, &ctx_), nullptr, "create");
+        ctx_ = dim3g_dropin::context();
         check(dim3g_mapper_create(ctx_, (uint64_t)(n > 0 ? n : 1), &m_), ctx_, "create");
     }
-    ~LS_mapper() {
-        dim3g_mapper_destroy(m_);
-        dim3g_destroy(ctx_);
-    }
+    ~LS_mapper() { dim3g_mapper_destroy(m_); }
     LS_mapper(const LS_mapper&) = delete;
     LS_mapper& operator=(const LS_mapper&) = delete;
 

@@ -58,6 +58,13 @@ struct myvector {
         reserve(size);
         cur_num = size;
     }
+    // Removes and returns the last element; an empty vector returns a
+    // value-initialised T (the reference returns NULL, which only compiles
+    // for pointer and arithmetic element types).
+    T pop_back() {
+        if (cur_num == 0) return T();
+        return data[--cur_num];
+    }
     inline _CountType size() const { return cur_num; }
     inline void clear() { cur_num = 0; }
 };

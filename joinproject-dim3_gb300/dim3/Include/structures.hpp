@@ -9,11 +9,23 @@
 
 #include <cstdint>
 
+#include "myBitVector.hpp"
+
 using LL = long long;
 using uLL = unsigned long long;
 
 struct myHasher {
     inline uint32_t operator()(const int key) const { return (uint32_t)key; }
+};
+
+// The dense part of S in the reference's hybrid layout (structures.hpp:14-20):
+// one bit vector per dense z over the y ids, with the z value and count.
+struct S_DENSE {
+    myBitVector<>* data;
+    int* id2v;
+    int* id2cnt;
+    int size;
+    int dense_bitvector_len;
 };
 
 template <typename _Tv = int>

@@ -16,6 +16,7 @@
 #include <bits/stdc++.h>
 
 #include "../../include/dim3gpu.h"
+#include "Include/dim3g_context.hpp"
 #include "Include/myvector.hpp"
 #include "Include/structures.hpp"
 
@@ -30,21 +31,6 @@ struct TUPLE {
 };
 
 namespace dim3g_dropin {
-
-// One context per process and device 0 (DIM3G_DEVICE selects another).
-inline dim3g_ctx* context() {
-    static dim3g_ctx* ctx = [] {
-        dim3g_ctx* c = nullptr;
-        const char* d = getenv("DIM3G_DEVICE");
-        int rc = dim3g_create(d ? atoi(d) : 0, &c);
-        if (rc != DIM3G_OK) {
-            printf("Fail to create the GPU join context (status %d).\n", rc);
-            exit(-1);
-        }
-        return c;
-    }();
-    return ctx;
-}
 
 inline void check(int rc, const char* what) {
     if (rc != DIM3G_OK) {
@@ -95,6 +81,30 @@ struct AggregateFunctionCount {
     inline _Tv get(const int key) const { return c[key]; }
 };
 
+// The reference's shipped AVG(R.v + S.v) plug-in (dim3.hpp:1453-1480), with
+// its interface: a float sum and a count per z, get = sum / count.  The GPU
+// path has no AVG kernel: DIM3JoinAggregate with this plug-in compiles (so
+// join_aggregate.cpp builds unchanged) and reports DIM3G_ERR_UNSUPPORTED at
+// run time, the reference's print-and-exit error behaviour.
+template <typename _Tv>
+struct AggregateFunctionAvg {
+    std::pair<_Tv, int>* acc;
+    AggregateFunctionAvg(int len) {
+        acc = (std::pair<_Tv, int>*)malloc((size_t)(len > 0 ? len : 1) * sizeof(std::pair<_Tv, int>));
+        if (!acc) {
+            printf("Fail to malloc the AVG accumulators.\n");
+            exit(-1);
+        }
+    }
+    ~AggregateFunctionAvg() { free(acc); }
+    inline void insert(const int key, const _Tv a, const _Tv b) { acc[key] = {a + b, 1}; }
+    inline void update(const int key, const _Tv a, const _Tv b) {
+        acc[key].first += a + b;
+        acc[key].second++;
+    }
+    inline _Tv get(const int key) const { return acc[key].first / acc[key].second; }
+};
+
 template <class A>
 struct dim3g_is_count : std::false_type {};
 template <class V>
@@ -104,10 +114,15 @@ template <typename _Tx, typename _Ty, typename _Tz, typename _Tv, typename _Aggr
           typename _Hy = hash<_Ty>, typename _Hz = hash<_Tz>, typename _Hxz = hash<pair<_Tx, _Tz>>,
           typename _Tcounter = uint32_t>
 struct DIM3JoinAggregate {
-    static_assert(dim3g_is_count<_Aggregate_type>::value, "the GPU path implements the COUNT aggregate");
-    static_assert(std::is_integral<_Tv>::value, "COUNT needs an integer value type");
+    static_assert(!dim3g_is_count<_Aggregate_type>::value || std::is_integral<_Tv>::value,
+                  "COUNT needs an integer value type");
     static void doJoinAggregate(myvector<TUPLE<_Tx, _Ty, _Tv>, _Tcounter>& R, myvector<TUPLE<_Tz, _Ty, _Tv>, _Tcounter>& S,
                                 myvector<TUPLE<_Tx, _Tz, _Tv>, _Tcounter>& result) {
+        if (!dim3g_is_count<_Aggregate_type>::value) {
+            printf("Fail in doJoinAggregate: only the COUNT aggregate runs on the GPU path (status %d).\n",
+                   DIM3G_ERR_UNSUPPORTED);
+            exit(-1);
+        }
         std::vector<uint32_t> r(2 * (size_t)R.size()), s(2 * (size_t)S.size());
         for (size_t i = 0; i < R.size(); i++) {
             r[2 * i] = (uint32_t)R.data[i].x;
@@ -128,7 +143,7 @@ struct DIM3JoinAggregate {
             printf("Fail to malloc the join-aggregate result.\n");
             exit(-1);
         }
-        for (uint64_t i = 0; i < n; i++) data[i] = T((_Tx)xz[2 * i], (_Tz)xz[2 * i + 1], (_Tv)cnt[i]);
+        for (uint64_t i = 0; i < n; i++) data[i] = T((_Tx)xz[2 * i], (_Tz)xz[2 * i + 1], (_Tv)(uint64_t)cnt[i]);
         free(xz);
         free(cnt);
         dim3g_dropin::adopt(result, data, n);
@@ -151,5 +166,24 @@ inline void gen_rand_data(myvector<pair<int, int>>& R, myvector<pair<int, int>>&
         int z = e() % MODZ;
         int y = e() % MODY;
         S.push_back({z, y});
+    }
+}
+
+// The reference's generator for valued tuples (dim3.hpp:1570-1591): the same
+// keys as above, each tuple's value its index as a float.
+inline void gen_rand_data(myvector<TUPLE<int, int, float>>& R, myvector<TUPLE<int, int, float>>& S, int nR = 1e7,
+                          int nS = 1e7, int MODX = 1e6, int MODY = 1e6, int MODZ = 1e6, int seed = 492) {
+    R.clear();
+    S.clear();
+    minstd_rand0 e(seed);
+    for (int i = 0; i < nR; i++) {
+        int x = e() % MODX;
+        int y = e() % MODY;
+        R.push_back(TUPLE<int, int, float>(x, y, (float)i));
+    }
+    for (int i = 0; i < nS; i++) {
+        int z = e() % MODZ;
+        int y = e() % MODY;
+        S.push_back(TUPLE<int, int, float>(z, y, (float)i));
     }
 }

@@ -5,6 +5,7 @@
     python run_case.py --mode batch [--queries 512]          # the mixed batch, one CUDA graph
     python run_case.py --mode relset_pass [--scale 1.0]      # 64 requests over the served set
     python run_case.py --workload zipf_1m --mode autotune    # the autotuner's choice for a workload
+    python run_case.py --mode project --a-tiles 64 --a-tile 0  # R's rows of one A-tile, all of S
 
 Prints one JSON line.  Used for profiling single launches (`ncu ...
 python run_case.py ...`): --mode count runs the mapping, CSR and count pass
@@ -95,6 +96,9 @@ def main():
     ap.add_argument("--tile-lo", type=int, default=0)
     ap.add_argument("--tile-hi", type=int, default=1)
     ap.add_argument("--queries", type=int, default=512)
+    ap.add_argument("--a-tiles", type=int, default=1,
+                    help="keep only R's rows in A-tile --a-tile of this many (fmix32(a) & (tiles-1)); S stays whole")
+    ap.add_argument("--a-tile", type=int, default=0)
     args = ap.parse_args()
     import torch
     ctx = dim3gpu.Context(0)
@@ -112,6 +116,12 @@ def main():
         ctx.close()
         return
     R, S = dim3gpu.workload(args.workload, args.scale)
+    if args.a_tiles > 1:
+        # an A-slice keeps the heavy rows' shape (same z domain, same S) at
+        # 1/a_tiles of the output: a representative case small enough to
+        # profile section by section
+        sel = (dim3gpu.fmix32_np(R[:, 0]) & np.uint64(args.a_tiles - 1)) == np.uint64(args.a_tile)
+        R = np.ascontiguousarray(R[sel])
     dR = _dev(R)
     dS = _dev(S)
     torch.cuda.synchronize()

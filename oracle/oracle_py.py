@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libdim3oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdim3ref.so")
-REF_SRC = "/root/reference"
+# The reference sources (present only where the fixtures are made);
+# DIM3_REFERENCE_SRC overrides the default location.
+REF_SRC = os.environ.get("DIM3_REFERENCE_SRC", "/root/reference")
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -337,6 +339,25 @@ def ref_join_project(R, S, parallel=False):
     out = ctypes.POINTER(ctypes.c_int)()
     n = L.ref_join_project(_ip(R), R.shape[0], _ip(S), S.shape[0], int(parallel), ctypes.byref(out))
     return _ref_take(L, out, n, 2)
+
+
+def ref_join_project_hash(R, S, chunk=1 << 26):
+    """The reference's join-project reduced to (|Result|, set hash), hashed in
+    chunks straight from its own result buffer (no copy), so results of
+    billions of pairs fit in host memory."""
+    L = ref()
+    R = np.ascontiguousarray(R, dtype=np.uint32).view(np.int32)
+    S = np.ascontiguousarray(S, dtype=np.uint32).view(np.int32)
+    out = ctypes.POINTER(ctypes.c_int)()
+    n = L.ref_join_project(_ip(R), R.shape[0], _ip(S), S.shape[0], 0, ctypes.byref(out))
+    h = 0
+    if n:
+        a = np.ctypeslib.as_array(out, shape=(n * 2,)).view(np.uint32).reshape(-1, 2)
+        for i in range(0, n, chunk):
+            h = (h + set_hash(a[i:i + chunk])) & 0xFFFFFFFFFFFFFFFF
+    if out:
+        L.ref_free(ctypes.cast(out, ctypes.c_void_p))
+    return int(n), h
 
 
 def ref_classical(R, S):

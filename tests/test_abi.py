@@ -77,3 +77,21 @@ def test_stats_struct_matches_header(tmp_path):
     got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
     assert got[0] == ctypes.sizeof(dim3gpu.Stats)
     assert got[1:] == [getattr(dim3gpu.Stats, f).offset for f in fields]
+
+
+def test_noalloc_rejects_misaligned_pointers_before_any_gpu_work(built):
+    """The allocation-free entry point reads and writes pairs as 8-byte
+    words: a pointer off that alignment is refused with DIM3G_ERR_INVALID
+    before any CUDA call (this runs without a GPU, so a call that reached
+    the runtime would report DIM3G_ERR_CUDA instead)."""
+    import dim3gpu
+    lib = ctypes.CDLL(dim3gpu.LIB_PATH)
+    vp, u64 = ctypes.c_void_p, ctypes.c_uint64
+    fn = lib.dim3g_join_project_noalloc
+    fn.argtypes = [vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64), vp]
+    n = u64(7)
+    good, off = 0x10000, 0x10004  # never dereferenced: the check comes first
+    for r, s, o in ((off, good, good), (good, off, good), (good, good, off)):
+        n.value = 7
+        assert fn(vp(r), 10, vp(s), 10, vp(o), 100, ctypes.byref(n), None) == dim3gpu.ERR_INVALID
+        assert n.value == 0

@@ -81,3 +81,18 @@ def test_oracle_restatement_matches_reference_order(built):
     rp, rc = O.ref_join_count(R, S)
     op, oc, n, h, st = O.join_count(R, S)
     assert np.array_equal(rp, op) and np.array_equal(rc, oc)
+
+
+def test_oracle_full_size_zipf_1m_matches_reference(built, golden):
+    """Config 1 at full size (1M x 1M, 2.36e9 distinct pairs): the oracle's
+    OpenMP form, hashing without storing pairs, against the reference's own
+    count and set hash (fixture zipf_1m_full)."""
+    import os
+
+    import dim3gpu
+    index, _ = golden
+    rec = index["zipf_1m_full"]
+    R, S = dim3gpu.workload("zipf_1m", 1.0)
+    assert str(input_hash(R, S)) == rec["input_hash"]
+    _, n, h, _ = O.join_project(R, S, threads=os.cpu_count() or 1, hash_only=True)
+    assert n == rec["n_out"] == 2356052933 and str(h) == rec["set_hash"]

@@ -89,6 +89,49 @@ def test_noalloc_rejects_results_beyond_its_pair_limit(built, golden):
     assert rc == dim3gpu.ERR_UNSUPPORTED and n == 0
 
 
+@pytest.mark.parametrize("na", [1024, 1025])
+def test_noalloc_pair_limit_is_exact(built, na):
+    """na x 1024 distinct pairs through one join value: exactly
+    DIM3G_NOALLOC_MAX_PAIRS (2^20) is accepted in full, one row more is
+    refused."""
+    import torch
+
+    import dim3gpu
+    from oracle import oracle_py as O
+
+    R = np.stack([np.arange(na, dtype=np.uint32), np.full(na, 5, np.uint32)], 1)
+    S = np.stack([np.arange(1024, dtype=np.uint32) + 7, np.full(1024, 5, np.uint32)], 1)
+    lib = dim3gpu.load()
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    cap = na * 1024
+    out = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    rc, n = _noalloc(lib, dR.data_ptr(), na, dS.data_ptr(), 1024, out.data_ptr(), cap, 0)
+    if na * 1024 <= (1 << 20):
+        assert rc == dim3gpu.OK and n == na * 1024
+        got = np.sort(O.pair_keys(out.cpu().numpy().view(np.uint32)))
+        want = np.sort((np.repeat(np.arange(na, dtype=np.uint64), 1024) << np.uint64(32))
+                       | np.tile(np.arange(1024, dtype=np.uint64) + np.uint64(7), na))
+        assert np.array_equal(got, want)
+    else:
+        assert rc == dim3gpu.ERR_UNSUPPORTED and n == 0
+
+
+def test_noalloc_empty_input_is_empty_whatever_the_other_size(built):
+    """An empty relation joins to nothing, even beside one above the size
+    limit (the same answer as dim3g_join_project_device)."""
+    import torch
+
+    import dim3gpu
+
+    lib = dim3gpu.load()
+    big = (1 << 18) + 1
+    d = torch.zeros((big, 2), dtype=torch.int32, device="cuda")
+    out = torch.empty((16, 2), dtype=torch.int32, device="cuda")
+    rc, n = _noalloc(lib, d.data_ptr(), big, d.data_ptr(), 0, out.data_ptr(), 16, 0)
+    assert rc == dim3gpu.OK and n == 0
+
+
 def test_noalloc_reports_capacity(built, golden):
     import torch
 
