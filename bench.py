@@ -52,6 +52,12 @@ WORKLOADS = {
 }
 
 
+# The tensor roofline's peak: the product kernel's own ceiling on this
+# device, measured by dim3g_calibrate (the measured peaks file holds bf16
+# cuBLAS only; the product runs fp8 e4m3 operands with f32 accumulators).
+FP8_PEAK_KIND = "measured: k_dense_mma (tcgen05 kind::f8f6f4) on all-ones operands, K = 4096, 8 tiles per SM"
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -128,9 +134,17 @@ def a_slice(R, parts, which):
     return np.ascontiguousarray(R[(h % np.uint64(parts)) == which])
 
 
+def host_threads():
+    """Cores this process may run on (`nproc`): THREAD_NUM of the OpenMP arm."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def cpu_run(R, S, parts, which, threads):
-    """One oracle DIM3_parallel run on an A-slice; the slice stays the larger
-    input so the output orientation is (a, c)."""
+    """One oracle run on an A-slice: DIM3_parallel with `threads` OpenMP
+    threads, or DIM3 serial for threads = 1."""
     from oracle import oracle_py
     Rs = a_slice(R, parts, which)
     t = time.perf_counter()
@@ -141,10 +155,21 @@ def cpu_run(R, S, parts, which, threads):
     return n, dt, st
 
 
+def serial_arm(args, R, S):
+    """The reference's single-threaded path (DIM3::doJoinProject, main.cpp:19),
+    as the oracle port, on a 1/(cpu_parts * serial_div) A-slice."""
+    import platform
+    parts = args.cpu_parts * args.serial_div
+    n, dt, _ = cpu_run(R, S, parts, 0, 1)
+    return {"value": round(n / dt / 1e6, 3), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "1/%d A-slice of %s (full S): %d pairs in %.2f s; oracle port of DIM3 (serial), %s"
+                      % (parts, args.workload, n, dt, platform.machine())}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
+    threads = host_threads()
     R, S = make_workload(args.workload)
     parts = args.cpu_parts
     for w in range(args.warmup):
@@ -155,25 +180,32 @@ def run_reference(args, rank, world):
         tot_n += n
         tot_t += dt
     value = tot_n / tot_t / 1e6
-    sample = "1/%d A-slice of %s per step (full S), oracle port of DIM3_parallel" % (parts, args.workload)
+    sample = ("1/%d A-slice of %s per step (full S), oracle port of DIM3_parallel, THREAD_NUM = nproc = %d"
+              % (parts, args.workload, threads))
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "sample": sample},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "thread_num": threads, "nproc": threads,
+                             "single_thread": serial_arm(args, R, S) if args.serial_div > 0 else None},
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def cpu_baseline(args):
-    threads = os.cpu_count() or 1
+    """The reference's OpenMP path (DIM3_parallel, THREAD_NUM = nproc) and its
+    single-threaded path, both as the oracle port, each on a bounded A-slice
+    of the same workload, timed on this host's cores."""
+    threads = host_threads()
     R, S = make_workload(args.workload)
     parts = args.cpu_parts
     n, dt, st = cpu_run(R, S, parts, 0, threads)
     return {"value": round(n / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "thread_num": threads, "nproc": threads,
             "sample": "1/%d A-slice of %s (full S): %d pairs in %.2f s; oracle port of DIM3_parallel, %d threads"
-                      % (parts, args.workload, n, dt, threads)}
+                      % (parts, args.workload, n, dt, threads),
+            "single_thread": serial_arm(args, R, S) if args.serial_div > 0 else None}
 
 
 def run_gpu(args, rank, world, local_rank):
@@ -191,6 +223,9 @@ def run_gpu(args, rank, world, local_rank):
     ctx = dim3gpu.Context(local_rank)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    # the device's own product rates and bandwidth for the dense block's
+    # cost model; the fp8 rate is also the tensor roofline's peak
+    cal = ctx.calibrate()
     dR = torch.from_numpy(R.view(np.int32)).cuda()
     dS = torch.from_numpy(S.view(np.int32)).cuda()
     torch.cuda.synchronize()
@@ -292,9 +327,9 @@ def run_gpu(args, rank, world, local_rank):
         ach_t = flops / (ms_t / 1e3) / 1e12
         bf16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops") \
             if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
-        tensor = {"bound": "tensor", "kernel": "k_dense_mma", "achieved": round(ach_t, 1), "peak": 4500.0,
-                  "peak_kind": "nominal fp8 dense (the measured peaks are bf16 only)", "unit": "TFLOP/s",
-                  "frac": round(ach_t / 4500.0, 4),
+        peak_t = cal["fp8_tflops"]
+        tensor = {"bound": "tensor", "kernel": "k_dense_mma", "achieved": round(ach_t, 1), "peak": peak_t,
+                  "peak_kind": FP8_PEAK_KIND, "unit": "TFLOP/s", "frac": round(ach_t / peak_t, 4),
                   "vs_measured_bf16_burst": round(ach_t / bf16, 4) if bf16 else None,
                   "flops_per_launch": int(flops), "ms_per_launch": round(ms_t, 3), "rows": st["rows_dense"],
                   "heavy_y": st["heavy_y"], "kp": st["dense_kp"]}
@@ -314,6 +349,7 @@ def run_gpu(args, rank, world, local_rank):
                      "expansion_all_classes": {"alg_bytes": int(alg_all), "ms": round(ms_w, 3),
                                                "achieved": round(alg_all / (ms_w / 1e3) / 1e9, 1)}},
         "roofline_tensor": tensor,
+        "calibration": cal,
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -426,6 +462,7 @@ def run_count16m(args, rank, world, local_rank):
     ctx = dim3gpu.Context(local_rank)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    cal = ctx.calibrate()
     dR = torch.from_numpy(R.view(np.int32)).cuda()
     dS = torch.from_numpy(S.view(np.int32)).cuda()
     tiles = 16
@@ -457,9 +494,9 @@ def run_count16m(args, rank, world, local_rank):
         sel = (O.fmix32(R[:, 0]) & np.uint64(4095)).astype(np.int64) == 0
         Rs = np.ascontiguousarray(R[sel])
         t = time.perf_counter()
-        _, _, ng, _, _ = O.join_count(S, Rs, threads=os.cpu_count() or 1, hash_only=True)
+        _, _, ng, _, _ = O.join_count(S, Rs, threads=host_threads(), hash_only=True)
         dt = time.perf_counter() - t
-        cpu = {"value": round(ng / dt / 1e6, 3), "unit": "Mgroups/s", "cores": os.cpu_count() or 1,
+        cpu = {"value": round(ng / dt / 1e6, 3), "unit": "Mgroups/s", "cores": host_threads(),
                "kind": "port", "sample": "1/4096 A-slice of count16m (full S): %d groups in %.2f s" % (ng, dt)}
     # expansion of the slices: 4 B per candidate read, nothing written
     alg = 4 * outj
@@ -468,8 +505,8 @@ def run_count16m(args, rank, world, local_rank):
         # group-hash epilogue is the dominant kernel
         ach = flops / (ms_mma / 1e3) / 1e12
         roof = {"bound": "tensor", "kernel": "k_dense_mma (COUNT summary epilogue)", "achieved": round(ach, 1),
-                "peak": 4500.0, "peak_kind": "nominal fp8 dense (the measured peaks are bf16 only)",
-                "unit": "TFLOP/s", "frac": round(ach / 4500.0, 4), "traffic": None,
+                "peak": cal["fp8_tflops"], "peak_kind": FP8_PEAK_KIND,
+                "unit": "TFLOP/s", "frac": round(ach / cal["fp8_tflops"], 4), "traffic": None,
                 "flops_per_launch": int(flops / max(args.steps, 1)), "ms_per_launch": round(ms_mma / args.steps, 3),
                 "kp": st["dense_kp"], "note": "the epilogue's two splitmix64 hashes per group bound the tile rate"}
     else:
@@ -484,7 +521,7 @@ def run_count16m(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64", "data": "synthetic",
         "config": {"workload": "count16m", "desc": WORKLOADS["count16m"], "groups": groups, "out_j": outj,
                    "slices": args.steps, "l2": "relations > L2; no flush"},
-        "roofline": roof,
+        "roofline": roof, "calibration": cal,
         "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": None,
     }
     if rank == 0:
@@ -624,6 +661,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="chung_lu_20m", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-parts", type=int, default=64)
+    ap.add_argument("--serial-div", type=int, default=4,
+                    help="the single-threaded arm takes a 1/(cpu-parts * serial-div) A-slice (0: skip it)")
     ap.add_argument("--traffic", type=float, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-queries", type=int, default=512)

@@ -295,14 +295,21 @@ void dim3g_batch_destroy(dim3g_batch* b);
  * Replaces server_parameter_estimator.cpp:77-269 and the cost models that
  * consume its constants (dim3.hpp:42-186): instead of machine constants fed
  * to a model, the join is timed on the caller's device-resident input under
- * candidate settings of the knobs that set the row classes' thresholds and
- * tile shapes (tile_bits_log2, block_threads, block_slots_log2,
- * warp_slots_log2) and the CTA rows' walk (cta_walk), by
- * coordinate descent from the context's current
- * settings (always a trial), and the fastest are applied to the context.
- * max_trials bounds the joins run (0: no bound). */
+ * candidate settings of the knobs that set the dense/sparse split
+ * (dense_block: the heavy rows through the tensor-core product or the sparse
+ * kernels; dense_k_max: how many of the heaviest join values the product
+ * takes -- the threshold on a join value's candidate mass), the row classes'
+ * thresholds and tile shapes (tile_bits_log2, block_threads,
+ * block_slots_log2, warp_slots_log2) and the CTA rows' walk (cta_walk), by
+ * coordinate descent from the context's current settings (always a trial),
+ * and the fastest are applied to the context.  The trial that runs the
+ * heavy rows on the sparse kernels also sets the context's measured sparse
+ * rate, which the dense block's cost model uses from then on (see
+ * dim3g_calibrate for the product's rates).  max_trials bounds the joins run
+ * (0: no bound). */
 typedef struct {
     int32_t tile_bits_log2, block_threads, block_slots_log2, warp_slots_log2, cta_walk;
+    int32_t dense_block, dense_k_max;
     float ms;          /* best measured device ms of one join */
     float ms_default;  /* the starting settings' ms */
     uint32_t trials;   /* settings timed */
@@ -318,6 +325,20 @@ int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out)
  * row>"), from one count pass; key_len >= 32. */
 int dim3g_tuning_key(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint32_t* d_S, uint64_t nS, char* key,
                      uint64_t key_len);
+/* Measures, on this context's device, the rates the dense block's cost
+ * model decides with, and makes that model use them (replacing the built-in
+ * defaults, which were measured once on a GB300): the tcgen05 fp8 product's
+ * throughput on all-ones operands at K = 4096 (fp8_tflops: the ceiling of
+ * k_dense_mma, dense flops 2 M N K per second), its fixed time per 128 x 256
+ * tile at K = 128 (tile_us: TMA fill and epilogue), and a device-to-device
+ * copy's bandwidth (hbm_gbs, read + write bytes).  Allocates about 100 MB of
+ * workspace; a few ms. */
+typedef struct {
+    float fp8_tflops, tile_us, hbm_gbs;
+    float sparse_gbs;  /* the sparse kernels' rate in the cost model (4 B a candidate) */
+} dim3g_calibration;
+int dim3g_calibrate(dim3g_ctx* ctx, dim3g_calibration* out);
+
 /* Text cache of tunings by key (one line each; the last line of a key wins).
  * Host-only; DIM3G_ERR_INVALID when the file or key is absent. */
 int dim3g_tuning_save(const char* path, const char* key, const dim3g_tuning* t);

@@ -828,6 +828,13 @@ int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out)
     const int r3 = r2 ? r2 : batch_capture(b);
     if (r) return r;
     if (r3) return r3;
+    {
+        int64_t db = 0, dk = 0;
+        dim3g_get_param(ctx, "dense_block", &db);
+        dim3g_get_param(ctx, "dense_k_max", &dk);
+        out->dense_block = (int32_t)db;  // not swept: batches run no dense block
+        out->dense_k_max = (int32_t)dk;
+    }
     out->cta_walk = (int32_t)best[0];
     out->block_slots_log2 = (int32_t)best[1];
     out->warp_slots_log2 = (int32_t)best[2];

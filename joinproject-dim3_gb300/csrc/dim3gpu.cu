@@ -73,6 +73,15 @@ struct Arena {
     }
 };
 
+// Rates of the dense block's cost model (run_dense).
+struct CostModel {
+    double tile_s = 0.8e-6;              // fixed time of one product tile (TMA fill, epilogue)
+    double sm_flops = 3.8e15 / 152;      // product rate of one SM
+    double dense_bw = 6.0e12;            // bitmap and light-pass streaming, bytes/s
+    double sparse_bw = 5.0e12;           // sparse expansion, 4 algorithmic bytes a candidate
+    bool calibrated = false;             // product rates and bandwidth measured on this device
+};
+
 struct Params {
     uint32_t warp_lg = 11;    // 2048 slots per warp set  -> class 1 up to 1024
     uint32_t block_lg = 14;   // 16384 slots per CTA set  -> class 2 up to 8192
@@ -111,6 +120,7 @@ struct dim3g_ctx {
     std::string err;
     Arena ws;
     Params prm;
+    CostModel cm;
     dim3g_stats stats{};
     // host-API staging (device) buffers, grow-only
     void* d_in = nullptr;
@@ -247,21 +257,20 @@ unsigned resident_grid(K kernel, int block, size_t smem, int sm) {
 // as one boolean product on the tensor cores (dense.cuh).  Cost model, in
 // seconds, against the bitmap-class expansion it replaces (4 algorithmic
 // bytes per candidate):
-//   product   tiles per SM x max(kDenseTileS, MMA time of a tile at
-//             kDenseSmFlops); the fixed part is a tile's TMA fill and
+//   product   tiles per SM x max(CostModel::tile_s, MMA time of a tile at
+//             CostModel::sm_flops); the fixed part is a tile's TMA fill and
 //             epilogue, which the MMAs hide from about Kp = 384 on
 //   bitmap    written by the product, read by the light pass and emission
 //   light     the candidates through the other join values, kLightBytes each
-// (constants measured on GB300, zipf_1m: 0.8 us a tile at Kp <= 256, about
-// 3.8 PFLOP/s for Kp = 384 .. 1024; the light pass 3-6 ps a candidate).
-constexpr double kDenseTileS = 0.8e-6;
+// The CostModel defaults were measured once on a GB300 (zipf_1m: 0.8 us a
+// tile at Kp <= 256, about 3.8 PFLOP/s for Kp = 384 .. 1024; the light pass
+// 3-6 ps a candidate); dim3g_calibrate replaces the product's rates and the
+// bandwidth with ones measured on the context's device, and the autotuner's
+// sparse trial the sparse rate.
 // summary epilogue, measured on the 16M x 16M Zipf-1.2 COUNT: ~32K group
 // hashes a tile (11.1 us) + 0.34 us per light candidate in the tile's bucket
 constexpr double kDenseTileSumS = 11.1e-6;
 constexpr double kDenseBucketS = 0.34e-6;
-constexpr double kDenseSmFlops = 3.8e15 / 152;
-constexpr double kDenseBw = 6.0e12;
-constexpr double kSparseBw = 5.0e12;
 constexpr double kLightBytes = 40.0;
 constexpr uint64_t kDenseMinCand = (uint64_t)1 << 26;  // smaller heavy work stays sparse (cost model mode)
 
@@ -356,15 +365,15 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
         if (kfit < kmax) kmax = kfit;
         if (kmax == 0) return DIM3G_OK;
     }
-    const double t_bitmap = 3.0 * (double)dbytes / kDenseBw;
+    const double t_bitmap = 3.0 * (double)dbytes / c->cm.dense_bw;
     const double ntile_all = (double)(Mp / kDenseBM) * (double)(Np / kDenseBN);
     const double tiles_per_sm = ceil(ntile_all / sm);
-    const double tile_fixed = bits ? kDenseTileS : kDenseTileSumS;
+    const double tile_fixed = bits ? c->cm.tile_s : kDenseTileSumS;
     auto t_product = [&](uint64_t Kp, double light) {
-        const double t_mma = 2.0 * kDenseBM * kDenseBN * (double)Kp / kDenseSmFlops;
+        const double t_mma = 2.0 * kDenseBM * kDenseBN * (double)Kp / c->cm.sm_flops;
         // summaries also count the operands in 32 bits first, and every
         // epilogue thread scans its tile's light bucket
-        const double t_ops = bits ? 0.0 : (double)(Mp + Np) * Kp * 9.0 / kDenseBw;
+        const double t_ops = bits ? 0.0 : (double)(Mp + Np) * Kp * 9.0 / c->cm.dense_bw;
         const double t_epi = tile_fixed + (bits ? 0.0 : kDenseBucketS * light / ntile_all);
         return tiles_per_sm * (t_mma > t_epi ? t_mma : t_epi) + t_ops;
     };
@@ -373,7 +382,7 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     const double t_min = t_product(kDenseBK, 0.0) + t_bitmap;
     // the sparse cost of all heavy rows bounds that of any prefix of them
     skip = 4;  // the cost model keeps the sparse path
-    if (mode == 1 && t_min >= (double)cd_all * 4.0 / kSparseBw) return DIM3G_OK;
+    if (mode == 1 && t_min >= (double)cd_all * 4.0 / c->cm.sparse_bw) return DIM3G_OK;
 
     CU(cudaEventRecord(c->evd[0], st));
     uint32_t* degd = ws_get<uint32_t>(c, k);
@@ -402,7 +411,7 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
     double sampled = 0;
     for (uint32_t b = 0; b < kDenseBins; b++) sampled += (double)hm[b] * step;
     const double cd = nd < n_heavy ? sampled : (double)cd_all;
-    const double t_sparse = cd * 4.0 / kSparseBw;
+    const double t_sparse = cd * 4.0 / c->cm.sparse_bw;
     // the heavy join values: whole bins from the top, at most kmax of them;
     // the cut with the lowest modelled cost (mode 2: the most)
     uint64_t kc = 0, best_k = 0;
@@ -416,7 +425,7 @@ int run_dense(dim3g_ctx* c, const JoinPlan& jp, const RowCtx& rc, Scalars* sc, c
         heavy += (double)hm[b] * step;
         const uint64_t Kp = round_up(kc, kDenseBK);
         const double light = sampled > heavy ? sampled - heavy : 0.0;
-        const double t = t_product(Kp, light) + t_bitmap + light * light_bytes / kDenseBw;
+        const double t = t_product(Kp, light) + t_bitmap + light * light_bytes / c->cm.dense_bw;
         // summaries: each epilogue thread scans its tile's light bucket, so
         // only cuts with a small average bucket qualify
         if (!bits && light > (double)ntile_all * kDenseBucketMax / 4 && b > 0) continue;
@@ -1090,6 +1099,9 @@ cudaStream_t stream(const dim3g_ctx* c) { return c->stream; }
 int device(const dim3g_ctx* c) { return c->device; }
 int sm_count(const dim3g_ctx* c) { return c->sm_count; }
 void add_launches(dim3g_ctx* c, uint64_t n) { c->launches += n; }
+void set_sparse_rate(dim3g_ctx* c, double bytes_per_s) {
+    if (bytes_per_s > 0) c->cm.sparse_bw = bytes_per_s;
+}
 int fail(dim3g_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -1364,6 +1376,79 @@ int dim3g_join_project_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, co
 int dim3g_join_count_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, const uint32_t* dS, uint64_t nS,
                              uint32_t tiles, uint32_t tile_lo, uint32_t tile_hi, dim3g_tile_summary* out) {
     return run_summary(c, dR, nR, dS, nS, true, tiles, tile_lo, tile_hi, out);
+}
+
+// The product kernel of the dense block on all-ones operands: a grid of
+// 8 tiles per SM of 128 x 256, at K = 4096 (the MMA rate) and at K = 128
+// (the fixed time of a tile), each the best of 5 launches timed with events
+// on the context's stream; then a device-to-device copy of 512 MB.
+int dim3g_calibrate(dim3g_ctx* c, dim3g_calibration* out) {
+    if (!c || !out) return DIM3G_ERR_INVALID;
+    memset(out, 0, sizeof *out);
+    CU(cudaSetDevice(c->device));
+    c->ws.reset();
+    cudaStream_t st = c->stream;
+    const int sm = c->sm_count;
+    const uint32_t nt = 16, mt = (uint32_t)(8 * sm + nt - 1) / nt;  // >= 8 tiles per SM
+    const uint64_t Mp = (uint64_t)mt * kDenseBM, Np = (uint64_t)nt * kDenseBN, Wd = Np / 32;
+    const uint32_t kmax = 4096;
+    uint8_t* A = ws_get<uint8_t>(c, Mp * kmax);
+    uint8_t* B = ws_get<uint8_t>(c, Np * kmax);
+    uint32_t* D = ws_get<uint32_t>(c, Mp * Wd);
+    unsigned int* err = ws_get<unsigned int>(c, 1);
+    const size_t copy_bytes = (size_t)512 << 20;
+    char* src = ws_get<char>(c, copy_bytes);
+    char* dst = ws_get<char>(c, copy_bytes);
+    if (!A || !B || !D || !err || !src || !dst) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (calibrate)");
+    CU(cudaMemsetAsync(A, kFp8One, Mp * kmax, st));
+    CU(cudaMemsetAsync(B, kFp8One, Np * kmax, st));
+    CU(cudaMemsetAsync(err, 0, 4, st));
+    CU(cudaMemsetAsync(src, 1, copy_bytes, st));
+    const uint32_t kps[2] = {kmax, kDenseBK};
+    float best[2] = {1e30f, 1e30f};
+    const unsigned grid = (unsigned)((uint64_t)mt * nt < (uint64_t)sm ? (uint64_t)mt * nt : (uint64_t)sm);
+    for (int which = 0; which < 2; which++) {
+        const uint32_t Kp = kps[which];
+        CUtensorMap mA, mB;
+        int r = dense_map(c, &mA, A, Mp, Kp, kDenseBM);
+        if (!r) r = dense_map(c, &mB, B, Np, Kp, kDenseBN);
+        if (r) return r;
+        for (int rep = 0; rep < 6; rep++) {  // the first launch warms up
+            CU(cudaEventRecord(c->evd[0], st));
+            k_dense_mma<kDenseBits><<<grid, kDenseThreads, kDenseSmem, st>>>(mA, mB, D, (uint32_t)Wd, mt, nt,
+                                                                              Kp / kDenseBK, err, DenseSum{});
+            CHECK_LAUNCH();
+            CU(cudaEventRecord(c->evd[1], st));
+            CU(cudaEventSynchronize(c->evd[1]));
+            float ms = 0;
+            CU(cudaEventElapsedTime(&ms, c->evd[0], c->evd[1]));
+            if (rep && ms < best[which]) best[which] = ms;
+        }
+    }
+    float copy_ms = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        CU(cudaEventRecord(c->evd[0], st));
+        CU(cudaMemcpyAsync(dst, src, copy_bytes, cudaMemcpyDeviceToDevice, st));
+        CU(cudaEventRecord(c->evd[1], st));
+        CU(cudaEventSynchronize(c->evd[1]));
+        float ms = 0;
+        CU(cudaEventElapsedTime(&ms, c->evd[0], c->evd[1]));
+        if (rep && ms < copy_ms) copy_ms = ms;
+    }
+    unsigned int h_err = 0;
+    CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
+    if (h_err) return fail(c, DIM3G_ERR_DEVICE, "calibration product reported flags %u", h_err);
+    const double tiles_per_sm = ceil((double)mt * nt / grid);
+    const double flops = 2.0 * (double)Mp * (double)Np * kmax;
+    out->fp8_tflops = (float)(flops / (best[0] * 1e-3) / 1e12);
+    out->tile_us = (float)(best[1] * 1e3 / tiles_per_sm);
+    out->hbm_gbs = (float)(2.0 * copy_bytes / (copy_ms * 1e-3) / 1e9);
+    c->cm.sm_flops = flops / (best[0] * 1e-3) / grid;
+    c->cm.tile_s = best[1] * 1e-3 / tiles_per_sm;
+    c->cm.dense_bw = 2.0 * copy_bytes / (copy_ms * 1e-3);
+    c->cm.calibrated = true;
+    out->sparse_gbs = (float)(c->cm.sparse_bw / 1e9);
+    return DIM3G_OK;
 }
 
 }  // extern "C"

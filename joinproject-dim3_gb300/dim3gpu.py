@@ -76,17 +76,26 @@ EXPORTS = [
     "dim3g_relset_pair_outj", "dim3g_server_create", "dim3g_server_submit", "dim3g_server_wait",
     "dim3g_server_release", "dim3g_server_stats", "dim3g_server_destroy",
     "dim3g_autotune", "dim3g_tuning_apply", "dim3g_tuning_key", "dim3g_tuning_save", "dim3g_tuning_load",
-    "dim3g_join_project_summary", "dim3g_join_count_summary", "dim3g_batch_autotune",
+    "dim3g_join_project_summary", "dim3g_join_count_summary", "dim3g_batch_autotune", "dim3g_calibrate",
 ]
 
 
 class Tuning(ctypes.Structure):
     _fields_ = [("tile_bits_log2", ctypes.c_int32), ("block_threads", ctypes.c_int32),
                 ("block_slots_log2", ctypes.c_int32), ("warp_slots_log2", ctypes.c_int32),
-                ("cta_walk", ctypes.c_int32), ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
+                ("cta_walk", ctypes.c_int32), ("dense_block", ctypes.c_int32), ("dense_k_max", ctypes.c_int32),
+                ("ms", ctypes.c_float), ("ms_default", ctypes.c_float), ("trials", ctypes.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Calibration(ctypes.Structure):
+    _fields_ = [("fp8_tflops", ctypes.c_float), ("tile_us", ctypes.c_float), ("hbm_gbs", ctypes.c_float),
+                ("sparse_gbs", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: round(float(getattr(self, k)), 4) for k, _ in self._fields_}
 
 
 class Result(ctypes.Structure):
@@ -182,6 +191,7 @@ def load(path=LIB_PATH):
     L.dim3g_tuning_save.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
     L.dim3g_tuning_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, tp]
     L.dim3g_batch_autotune.argtypes = [vp, ctypes.c_uint32, tp]
+    L.dim3g_calibrate.argtypes = [vp, ctypes.POINTER(Calibration)]
     for f in (L.dim3g_join_project_summary, L.dim3g_join_count_summary):
         f.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                       _u64p]
@@ -306,6 +316,13 @@ class Context:
         t = Tuning()
         self._check(self.L.dim3g_autotune(self.h, _ptr(dR), nR, _ptr(dS), nS, max_trials, ctypes.byref(t)))
         return t.as_dict()
+
+    def calibrate(self):
+        """Measure the dense block's product rates and the copy bandwidth on
+        this device and use them in its cost model (see dim3g_calibrate)."""
+        cal = Calibration()
+        self._check(self.L.dim3g_calibrate(self.h, ctypes.byref(cal)))
+        return cal.as_dict()
 
     def apply_tuning(self, t):
         tt = Tuning(**{k: t[k] for k, _ in Tuning._fields_})

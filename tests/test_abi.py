@@ -44,22 +44,25 @@ def test_tuning_cache_roundtrip(built, tmp_path):
     path = str(tmp_path / "tuning.txt")
     assert dim3gpu.tuning_load(path, "p24_z20_w3") is None
     a = {"tile_bits_log2": 18, "block_threads": 256, "block_slots_log2": 13, "warp_slots_log2": 10,
-         "cta_walk": 1, "ms": 12.5, "ms_default": 14.0, "trials": 9}
+         "cta_walk": 1, "dense_block": 2, "dense_k_max": 512, "ms": 12.5, "ms_default": 14.0, "trials": 9}
     b = dict(a, tile_bits_log2=19, ms=11.0)
     dim3gpu.tuning_save(path, "p24_z20_w3", a)
     dim3gpu.tuning_save(path, "p20_z16_w5", dict(a, warp_slots_log2=9))
     dim3gpu.tuning_save(path, "p24_z20_w3", b)
     got = dim3gpu.tuning_load(path, "p24_z20_w3")
     assert got["tile_bits_log2"] == 19 and abs(got["ms"] - 11.0) < 1e-3 and got["trials"] == 9
+    assert got["dense_block"] == 2 and got["dense_k_max"] == 512
     assert dim3gpu.tuning_load(path, "p20_z16_w5")["warp_slots_log2"] == 9
     assert dim3gpu.tuning_load(path, "nope") is None
     with pytest.raises(dim3gpu.Dim3GError):
         dim3gpu.tuning_save(path, "has space", a)
 
 
-def test_stats_struct_matches_header(tmp_path):
-    """The ctypes mirror of dim3g_stats has the header struct's size and
-    field offsets (a C probe compiled against include/dim3gpu.h)."""
+@pytest.mark.parametrize("cname,pyname", [("dim3g_stats", "Stats"), ("dim3g_tuning", "Tuning"),
+                                          ("dim3g_calibration", "Calibration")])
+def test_struct_mirrors_match_header(tmp_path, cname, pyname):
+    """The ctypes mirror of a header struct has its size and field offsets
+    (a C probe compiled against include/dim3gpu.h)."""
     import shutil
     import subprocess
     import ctypes
@@ -67,16 +70,18 @@ def test_stats_struct_matches_header(tmp_path):
     if shutil.which("gcc") is None:
         pytest.skip("no C compiler")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    fields = [f for f, _ in dim3gpu.Stats._fields_]
+    py = getattr(dim3gpu, pyname)
+    fields = [f for f, _ in py._fields_]
     src = tmp_path / "probe.c"
     src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"dim3gpu.h\"\nint main(void){\n"
-                   "printf(\"%zu\\n\", sizeof(dim3g_stats));\n"
-                   + "".join("printf(\"%%zu\\n\", offsetof(dim3g_stats, %s));\n" % f for f in fields) + "return 0;}\n")
+                   "printf(\"%%zu\\n\", sizeof(%s));\n" % cname
+                   + "".join("printf(\"%%zu\\n\", offsetof(%s, %s));\n" % (cname, f) for f in fields)
+                   + "return 0;}\n")
     exe = tmp_path / "probe"
     subprocess.check_call(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)])
     got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
-    assert got[0] == ctypes.sizeof(dim3gpu.Stats)
-    assert got[1:] == [getattr(dim3gpu.Stats, f).offset for f in fields]
+    assert got[0] == ctypes.sizeof(py)
+    assert got[1:] == [getattr(py, f).offset for f in fields]
 
 
 def test_noalloc_rejects_misaligned_pointers_before_any_gpu_work(built):

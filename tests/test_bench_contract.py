@@ -19,6 +19,9 @@ def test_reference_arm_line():
               "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["thread_num"] == cb["nproc"] == cb["cores"]
+    st = cb["single_thread"]  # the reference's serial path beside its OpenMP one
+    assert st["cores"] == 1 and st["value"] > 0 and st["unit"] == d["unit"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"] == "zipf_1m"

@@ -187,7 +187,8 @@ def test_autotune_applies_settings_and_keeps_results_exact(built, golden, tmp_pa
     assert key.startswith("p")
     t = c.autotune(dR, R.shape[0], dS, S.shape[0], max_trials=8)
     assert 1 <= t["trials"] <= 8 and t["ms"] <= t["ms_default"]
-    for k in ["tile_bits_log2", "block_threads", "block_slots_log2", "warp_slots_log2", "cta_walk"]:
+    for k in ["tile_bits_log2", "block_threads", "block_slots_log2", "warp_slots_log2", "cta_walk", "dense_block",
+              "dense_k_max"]:
         assert c.get_param(k) == t[k]
     check_pairs(c.join_project(R, S), index[name], arrays, name)
     path = str(tmp_path / "t.txt")
@@ -199,6 +200,36 @@ def test_autotune_applies_settings_and_keeps_results_exact(built, golden, tmp_pa
     check_groups(p, cnt, index[name], arrays, name)
     c.close()
     c2.close()
+
+
+@pytest.mark.parametrize("name,dense", [("zipf_1m_s01", True), ("chung_lu_s005", False)])
+def test_autotune_chooses_the_dense_sparse_split(built, golden, name, dense):
+    """The dense/sparse split is tuned by measurement: the tuner times the
+    heavy rows on the sparse kernels (dense_block 0), through the tensor-core
+    product (2) and by the calibrated cost model (1), then how many join
+    values the product takes (dense_k_max), and keeps the fastest.  The Zipf
+    case's heavy rows are dense (a product over its heaviest join values
+    beats expanding them); the 2-hop's are not (1 % output density in its
+    heavy rows).  Results under the choice are exact."""
+    import torch
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    cal = c.calibrate()
+    assert cal["fp8_tflops"] > 500 and cal["hbm_gbs"] > 1000 and cal["tile_us"] > 0
+    R, S = case_inputs(name, index, arrays)
+    dR = torch.from_numpy(R.view(np.int32)).cuda()
+    dS = torch.from_numpy(S.view(np.int32)).cuda()
+    t = c.autotune(dR, R.shape[0], dS, S.shape[0])
+    assert t["ms"] <= t["ms_default"]
+    assert c.get_param("dense_block") == t["dense_block"] and c.get_param("dense_k_max") == t["dense_k_max"]
+    n = c.join_project_count_device(dR, R.shape[0], dS, S.shape[0])
+    out = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    assert c.join_project_device(dR, R.shape[0], dS, S.shape[0], out, n) == n
+    took_dense = c.stats()["rows_dense"] > 0
+    assert took_dense == dense, (name, t, c.stats()["dense_skip"])
+    check_pairs(out.cpu().numpy().view(np.uint32), index[name], arrays, name)
+    c.close()
 
 
 @pytest.mark.parametrize("name", ["grd_small", "grd_swap", "heavy_duplicates", "zipf_1m_s001", "chung_lu_s005",
