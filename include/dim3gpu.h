@@ -85,7 +85,8 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * "cta_walk" (how CTA rows share candidates among warps: 0 = the row's
  * segment table staged in shared memory and its candidates split evenly,
  * 1 = warps take whole 32-entry chunks in turn, 2 = every chunk split
- * across the warps), "dense_block" (the heavy rows' join through their
+ * across the warps, 3 = every warp an equal share of the row's candidates
+ * over the chunks staged in shared memory), "dense_block" (the heavy rows' join through their
  * heaviest join values as one boolean product on the tensor cores: 0 off,
  * 1 when the cost model prefers it, 2 whenever its bitmap fits),
  * "dense_k_max" (32..4096: most join values in that product),

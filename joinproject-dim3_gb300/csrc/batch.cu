@@ -775,7 +775,7 @@ int dim3g_batch_autotune(dim3g_batch* b, uint32_t max_trials, dim3g_tuning* out)
         const char* name;
         std::vector<int64_t> values;
     };
-    const std::vector<K> knobs = {{"cta_walk", {0, 1, 2}},
+    const std::vector<K> knobs = {{"cta_walk", {3, 0, 1, 2}},
                                   {"block_slots_log2", {14, 13, 12}},
                                   {"warp_slots_log2", {11, 10, 9, 12}},
                                   {"block_threads", {512, 256, 1024}},

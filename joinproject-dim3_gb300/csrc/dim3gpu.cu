@@ -89,7 +89,7 @@ struct Params {
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     bool ordered = false;     // two-pass, rows in x-id order
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
-    uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split
+    uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split, 3 balanced
     uint32_t dense = 1;       // dense block on the tensor cores: 0 off, 1 by cost model, 2 whenever it fits
     uint32_t dense_k_max = 2048;  // most join values in the dense product
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
@@ -1217,7 +1217,7 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
         if (v < 10 || v > 20) return fail(c, DIM3G_ERR_INVALID, "tile_bits_log2 must be in 10..20");
         c->prm.tile_lg = (uint32_t)v;
     } else if (!strcmp(name, "cta_walk")) {
-        if (v < 0 || v > 2) return fail(c, DIM3G_ERR_INVALID, "cta_walk must be 0, 1 or 2");
+        if (v < 0 || v > 3) return fail(c, DIM3G_ERR_INVALID, "cta_walk must be 0, 1, 2 or 3");
         c->prm.cta_rr = (uint32_t)v;
     } else if (!strcmp(name, "host_direct_output")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "host_direct_output must be 0 or 1");

@@ -64,7 +64,7 @@ struct RowCtx {
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
-    uint32_t cta_rr;       // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split (cta_expand)
+    uint32_t cta_rr;       // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split, 3 balanced (cta_expand)
     const uint32_t* ucap;  // per row min(candidates, m)
     uint32_t* cnt;         // per row distinct count (count pass output)
     const unsigned long long* off;  // per row output offset (write pass input)
@@ -264,14 +264,16 @@ __device__ __forceinline__ void warp_expand(const RowCtx& c, uint32_t e0, uint32
 }
 
 // Chunks a CTA defers to its cooperative phase (round-robin walk), and the
-// staged segment table of the row-flattened walk (see cta_expand).
+// staged segment table of the row-flattened and balanced walks (see
+// cta_expand).
 constexpr uint32_t kBigChunk = 4096, kBigCap = 64;
-constexpr uint32_t kRowBlk = 1024;  // R entries staged at a time by the flattened walk
+constexpr uint32_t kRowBlk = 1024;  // R entries staged at a time by the flattened / balanced walks
 struct CtaChunks {
     uint32_t n;              // deferred chunks (may exceed kBigCap: the rest ran at once)
     uint32_t eb[kBigCap];
-    uint32_t s0[kRowBlk];    // flattened walk: segment start of each staged entry
-    uint32_t incl[kRowBlk];  // and the inclusive prefix of the segment lengths
+    uint32_t s0[kRowBlk];    // segment start of each staged entry
+    uint32_t incl[kRowBlk];  // flattened walk: inclusive prefix of the lengths; balanced walk: the lengths
+    uint32_t ctot[kRowBlk / 32];  // balanced walk: candidates of each staged 32-entry chunk
 };
 
 // Row-flattened CTA walk over R entries [e0, e1) and S tiles [t0, t1): the
@@ -359,9 +361,66 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
     }
 }
 
+// Balanced CTA walk over R entries [e0, e1) and S tiles [t0, t1): the warps
+// stage kRowBlk entries' segments in shared memory, each warp loading whole
+// 32-entry chunks (every entry is loaded once), then every warp takes an
+// equal share of the block's candidates -- the chunks overlapping its share,
+// each through expand_piece with the chunk rebuilt from shared memory -- so
+// no warp idles at the next barrier while another expands a long chunk
+// alone.  Contains barriers; called by the whole CTA.
+template <class Set, class Sink>
+__device__ __forceinline__ void cta_expand_balanced(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t t0,
+                                                    uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint64_t pol = l2_keep_policy();
+    for (uint32_t eb = e0; eb < e1; eb += kRowBlk) {
+        const uint32_t ne = min(kRowBlk, e1 - eb), nch = (ne + 31) >> 5;
+        for (uint32_t k = wib; k < nch; k += nw) {
+            const uint32_t i = k * 32 + lane, e = eb + i;
+            uint32_t s0 = 0, len = 0;
+            if (i < ne) {
+                const uint32_t y = ld_keep(&c.IC_R[e], pol);
+                const uint64_t r = (uint64_t)y * c.T;
+                s0 = ld_keep(&c.JR_S[r + t0], pol);
+                len = ld_keep(&c.JR_S[r + t1], pol) - s0;
+            }
+            cc->s0[i] = s0;
+            cc->incl[i] = len;
+            const uint32_t inc = warp_incl_scan(len);
+            if (__any_sync(0xffffffffu, inc < len)) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
+            if (lane == 31) cc->ctot[k] = inc;
+        }
+        __syncthreads();
+        // prefix of the chunk totals (every warp computes it; nch <= 32)
+        const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
+        const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
+        // first chunk holding candidate p0: chunks with incl <= p0 form a prefix
+        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
+            const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
+            const uint32_t cex = cin - ctot;
+            if (cex >= p1) break;
+            if (ctot == 0) continue;
+            Chunk ch;
+            ch.s0 = cc->s0[k * 32 + lane];
+            ch.len = cc->incl[k * 32 + lane];
+            ch.incl = warp_incl_scan(ch.len);
+            ch.excl = ch.incl - ch.len;
+            ch.total = ctot;
+            const uint32_t lo = p0 > cex ? p0 - cex : 0u, hi = p1 < cin ? p1 - cex : ctot;
+            expand_piece(c, ch, lo, hi, set, sink, pol);
+        }
+        __syncthreads();  // the staged table is rewritten by the next block
+    }
+}
+
 // CTA-level expansion of R entries [e0, e1) over S tiles [t0, t1), called
 // by all warps of the CTA (2^nw_lg of them) with the same arguments.
-// c.cta_rr selects the walk: 0 the row-flattened walk (cta_expand_flat),
+// c.cta_rr selects the walk: 3 the balanced walk (cta_expand_balanced),
+// 0 the row-flattened walk (cta_expand_flat),
 // 2 every chunk split across the warps (warp_expand), 1 with at least as
 // many chunks as warps, each warp takes whole
 // chunks round-robin -- a chunk's entries and segment bounds are loaded by
@@ -374,6 +433,10 @@ template <class Set, class Sink>
 __device__ __forceinline__ void cta_expand(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t wib, uint32_t nw_lg,
                                            uint32_t t0, uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
     const uint32_t nchunks = (e1 - e0 + 31) >> 5;
+    if (c.cta_rr == 3) {
+        cta_expand_balanced(c, e0, e1, t0, t1, set, sink, cc);
+        return;
+    }
     if (c.cta_rr == 0) {
         cta_expand_flat(c, e0, e1, t0, t1, set, sink, cc);
         return;

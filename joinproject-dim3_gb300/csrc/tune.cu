@@ -102,7 +102,7 @@ int dim3g_autotune(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uint3
                                {"block_threads", {512, 256, 1024}},
                                {"block_slots_log2", {14, 13, 12}},
                                {"warp_slots_log2", {11, 10, 9, 12}},
-                               {"cta_walk", {0, 1, 2}}};
+                               {"cta_walk", {3, 2, 0, 1}}};
     enum { kDenseKnob = 0, kDenseKKnob = 1 };
     std::vector<int64_t> cur(knobs.size());
     for (size_t i = 0; i < knobs.size(); i++) {

@@ -122,6 +122,33 @@ def test_kernel_classes_and_tiling_agree(built, golden, params):
     c.close()
 
 
+@pytest.mark.parametrize("walk", [0, 1, 2, 3])
+def test_cta_walks_agree(built, golden, walk):
+    """Every way a CTA row's candidates are shared among its warps gives the
+    same answer; small hash sets and narrow z tiles put most rows through the
+    CTA classes, with many tiles (projection, ordered projection, per-A-tile
+    summaries)."""
+    import torch
+    import dim3gpu
+    from oracle import oracle_py as O
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    for k, v in (("cta_walk", walk), ("warp_slots_log2", 6), ("block_slots_log2", 9), ("tile_bits_log2", 12)):
+        c.set_param(k, v)
+    for name in ["grd_small", "grd_sparse", "chung_lu_s005", "zipf_1m_s001", "heavy_duplicates", "one_join_value"]:
+        R, S = case_inputs(name, index, arrays)
+        check_pairs(c.join_project(R, S), index[name], arrays, name)
+        c.set_param("ordered_output", 1)
+        check_pairs(c.join_project(R, S), index[name], arrays, name)
+        c.set_param("ordered_output", 0)
+        dR = torch.from_numpy(R.view(np.int32)).cuda()
+        dS = torch.from_numpy(S.view(np.int32)).cuda()
+        got = c.join_project_summary(dR, R.shape[0], dS, S.shape[0], 16)
+        assert int(got[:, 0].sum()) == index[name]["n_out"]
+        assert str(int(got[:, 2].sum(dtype=np.uint64))) == index[name]["set_hash"]
+    c.close()
+
+
 def test_repeated_calls_are_stable(ctx, golden):
     index, arrays = golden
     R, S = case_inputs("chung_lu_s005", index, arrays)
@@ -202,15 +229,16 @@ def test_autotune_applies_settings_and_keeps_results_exact(built, golden, tmp_pa
     c2.close()
 
 
-@pytest.mark.parametrize("name,dense", [("zipf_1m_s01", True), ("chung_lu_s005", False)])
+@pytest.mark.parametrize("name,dense", [("grd_all_dense", True), ("chung_lu_s005", False)])
 def test_autotune_chooses_the_dense_sparse_split(built, golden, name, dense):
     """The dense/sparse split is tuned by measurement: the tuner times the
     heavy rows on the sparse kernels (dense_block 0), through the tensor-core
     product (2) and by the calibrated cost model (1), then how many join
-    values the product takes (dense_k_max), and keeps the fastest.  The Zipf
-    case's heavy rows are dense (a product over its heaviest join values
-    beats expanding them); the 2-hop's are not (1 % output density in its
-    heavy rows).  Results under the choice are exact."""
+    values the product takes (dense_k_max), and keeps the fastest.  The
+    all-dense case's heavy rows are dense (every (x, z) group exists: a
+    product over its heaviest join values beats expanding them); the 2-hop's
+    are not (1 % output density in its heavy rows).  Results under the
+    choice are exact."""
     import torch
     import dim3gpu
     index, arrays = golden
