@@ -16,6 +16,7 @@ enum DeviceError : uint32_t {
     kErrOutputBound = 4u,   // a write-pass position ran past the row's count
     kErrCountRange = 8u,    // a per-group count could exceed 32 bits
     kErrDenseTimeout = 16u, // a wait of the dense product ran out of time
+    kErrStreamTimeout = 32u,  // a wait of the streamed bitmap rows ran out of time
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }

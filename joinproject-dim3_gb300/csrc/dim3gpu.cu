@@ -31,6 +31,7 @@
 #include "mapping.cuh"
 #include "scan.cuh"
 #include "single.cuh"
+#include "stream.cuh"
 
 using namespace dim3g;
 
@@ -89,11 +90,12 @@ struct Params {
     uint32_t tile_lg = 19;    // 2^19-bit z tiles (64 KB bitmap)
     bool ordered = false;     // two-pass, rows in x-id order
     bool host_direct = true;  // pinned host outputs are written by the kernels directly
-    uint32_t cta_rr = 2;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split, 3 balanced
+    uint32_t cta_rr = 3;      // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split, 3 balanced
     uint32_t dense = 1;       // dense block on the tensor cores: 0 off, 1 by cost model, 2 whenever it fits
     uint32_t dense_k_max = 2048;  // most join values in the dense product
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
     bool keep_roles = false;  // R drives the join whatever the sizes (no swap)
+    uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
 };
 
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
@@ -785,8 +787,14 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
                 list_m, dp.nd, dp.D, dp.Wd, dp.Wm, dp.cpr, dp.coff, id2x, id2z, out, nullptr, &sc->dense_base);
             CHECK_LAUNCH();
         }
-        k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3, L.n4,
-                                                                                         bm_words);
+        if (c->prm.stream_rows) {
+            const size_t ss_s = stream_smem_bytes(bm_words);
+            k_stream_bitmap<<<resident_grid(k_stream_bitmap, kStreamThreads, ss_s, sm), kStreamThreads, ss_s, st>>>(
+                rc, rs, L.m, L.n3, L.n4, bm_words);
+        } else {
+            k_single_bitmap<<<resident_grid(k_single_bitmap, blk_m, ss_m, sm), blk_m, ss_m, st>>>(rc, rs, L.m, L.n3,
+                                                                                             L.n4, bm_words);
+        }
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[5], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[0], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
@@ -1151,6 +1159,8 @@ int dim3g_create(int device, dim3g_ctx** out) {
                                    ((1 << 14) + 32 * (int)kStage) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_stream_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)stream_smem_bytes(smem_m / 4)) == cudaSuccess &&
               cudaFuncSetAttribute(k_dense_mma<kDenseBits>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kDenseSmem) == cudaSuccess &&
               cudaFuncSetAttribute(k_dense_mma<kDenseSumProject>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1237,6 +1247,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "dense_mem_mb")) {
         if (v < 1 || v > (1 << 20)) return fail(c, DIM3G_ERR_INVALID, "dense_mem_mb must be in 1..2^20");
         c->prm.dense_mem = (uint64_t)v << 20;
+    } else if (!strcmp(name, "stream_rows")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "stream_rows must be 0 or 1");
+        c->prm.stream_rows = (uint32_t)v;
     } else if (!strcmp(name, "keep_roles")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "keep_roles must be 0 or 1");
         c->prm.keep_roles = v == 1;
@@ -1259,6 +1272,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "dense_k_max")) *v = c->prm.dense_k_max;
     else if (!strcmp(name, "dense_mem_mb")) *v = (int64_t)(c->prm.dense_mem >> 20);
     else if (!strcmp(name, "keep_roles")) *v = c->prm.keep_roles ? 1 : 0;
+    else if (!strcmp(name, "stream_rows")) *v = c->prm.stream_rows;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

@@ -28,11 +28,12 @@ struct Reserve {
 
 struct StageSink {
     static constexpr bool kValues = true;
-    uint32_t* stage;  // this warp's kStage-entry buffer
+    uint32_t* stage;  // this warp's buffer of `cap` entries
     uint2* out;
     Reserve rs;
     uint32_t xv;
-    uint32_t n = 0;  // staged entries (warp-uniform)
+    uint32_t n = 0;        // staged entries (warp-uniform)
+    uint32_t cap = kStage;  // at least 32 * kUnroll
 
     __device__ __forceinline__ void flush() {
         if (n == 0) return;
@@ -52,7 +53,7 @@ struct StageSink {
 #pragma unroll
         for (uint32_t u = 0; u < N; u++) tot += __popc(b[u]);
         if (tot == 0) return;
-        if (n + tot > kStage) flush();
+        if (n + tot > cap) flush();
         const uint32_t lt = lanemask_lt();
         uint32_t pos = n;
 #pragma unroll

@@ -149,6 +149,38 @@ def test_cta_walks_agree(built, golden, walk):
     c.close()
 
 
+@pytest.mark.parametrize("params", [
+    {"block_slots_log2": 9, "warp_slots_log2": 6, "tile_bits_log2": 10},
+    {"block_slots_log2": 9, "warp_slots_log2": 6, "tile_bits_log2": 14},
+    {"tile_bits_log2": 19},
+    {"tile_bits_log2": 20},
+])
+def test_streamed_bitmap_rows_agree(built, golden, params):
+    """The bitmap-class rows with their S segments streamed into shared
+    memory by bulk copies (stream_rows = 1): exact on every case, with many
+    narrow z tiles (segments split across stages, many tile ends) and with
+    the default and widest tiles; twice in a row on one context."""
+    import torch
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    c.set_param("stream_rows", 1)
+    for k, v in params.items():
+        c.set_param(k, v)
+    for name in CASES:
+        R, S = case_inputs(name, index, arrays)
+        for _ in range(2):
+            check_pairs(c.join_project(R, S), index[name], arrays, name)
+        if R.shape[0] and S.shape[0]:
+            dR = torch.from_numpy(R.view(np.int32)).cuda()
+            dS = torch.from_numpy(S.view(np.int32)).cuda()
+            n = index[name]["n_out"]
+            out = torch.empty((max(n, 1), 2), dtype=torch.int32, device="cuda")
+            assert c.join_project_device(dR, R.shape[0], dS, S.shape[0], out, out.shape[0]) == n
+            check_pairs(out[:n].cpu().numpy().view(np.uint32), index[name], arrays, name)
+    c.close()
+
+
 def test_repeated_calls_are_stable(ctx, golden):
     index, arrays = golden
     R, S = case_inputs("chung_lu_s005", index, arrays)
