@@ -150,8 +150,8 @@ def test_cta_walks_agree(built, golden, walk):
 
 
 @pytest.mark.parametrize("params", [
-    {"block_slots_log2": 9, "warp_slots_log2": 6, "tile_bits_log2": 10},
-    {"block_slots_log2": 9, "warp_slots_log2": 6, "tile_bits_log2": 14},
+    {"warp_slots_log2": 6, "block_slots_log2": 9, "tile_bits_log2": 10},
+    {"warp_slots_log2": 6, "block_slots_log2": 9, "tile_bits_log2": 14},
     {"tile_bits_log2": 19},
     {"tile_bits_log2": 20},
 ])
