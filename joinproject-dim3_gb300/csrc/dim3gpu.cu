@@ -644,8 +644,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cnt_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* cur_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* JR_S = ws_get<uint32_t>(c, nyt + 1);
-    uint32_t* IC_S = ws_get<uint32_t>(c, nq);
-    uint32_t* VS = ws_get<uint32_t>(c, nq);
+    // +4: the streamed bitmap rows copy 16-byte-aligned supersets of S
+    // segments, up to 3 elements past the last one
+    uint32_t* IC_S = ws_get<uint32_t>(c, nq + 4);
+    uint32_t* VS = ws_get<uint32_t>(c, nq + 4);
     uint32_t* Zq = ws_get<uint32_t>(c, nq);
     uint32_t* ucap = ws_get<uint32_t>(c, n);
     uint8_t* cls = ws_get<uint8_t>(c, n);

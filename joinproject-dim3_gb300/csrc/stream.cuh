@@ -10,13 +10,12 @@
 //   producer (warp 0)  takes rows from the class's dynamic counter, reads the
 //                      row's S segment bounds for one tile 32 entries at a
 //                      time, and copies the segments' z ids and z values into
-//                      a ring of stages in shared memory: the 16-byte-aligned
-//                      interior of a segment with one cp.async.bulk per array
-//                      (completion counted on the stage's mbarrier), its
-//                      unaligned head and tail (at most 3 + 3 elements) with
-//                      plain loads; slots left over by alignment hold the
-//                      empty id.  A segment longer than kStreamPiece is cut
-//                      into pieces at aligned points.
+//                      a ring of stages in shared memory: one cp.async.bulk
+//                      per array of the segment's 16-byte-aligned superset
+//                      (completion counted on the stage's mbarrier); a valid
+//                      mask per stage marks the segment's own slots.  A
+//                      segment longer than kStreamPiece is cut into pieces at
+//                      aligned points.
 //   consumers          every consumer warp takes an equal slice of each
 //                      stage: test-and-set of the tile bitmap from shared
 //                      memory, first insertions staged per warp and written
@@ -39,7 +38,7 @@ constexpr uint32_t kStreamConsumers = 8;
 constexpr uint32_t kStreamThreads = 32 * (kStreamConsumers + 1);
 constexpr uint32_t kStreamStages = 4;
 constexpr uint32_t kStreamCap = 1024;   // slots per stage: 128 per consumer warp (4 steps of 32)
-constexpr uint32_t kStreamPiece = 496;  // longest piece of a segment placed at once (+ 8 alignment slots <= cap / 2)
+constexpr uint32_t kStreamPiece = 496;  // longest piece of a segment placed at once (+ 6 alignment slots <= cap / 2)
 constexpr uint32_t kStreamStageVals = 256;  // staged z values per consumer warp
 constexpr unsigned long long kStreamWaitNs = 2000000000ull;
 
@@ -58,6 +57,7 @@ struct StreamSmem {
     uint32_t z[kStreamStages][kStreamCap];
     uint32_t v[kStreamStages][kStreamCap];
     uint32_t stage[kStreamConsumers][kStreamStageVals];
+    uint32_t mask[kStreamStages][kStreamCap / 32];  // valid slots of each stage
     StreamHdr hdr[kStreamStages];
     unsigned long long full[kStreamStages], empty[kStreamStages];
     unsigned long long tdone, tclear;  // consumers: tile finished, bitmap cleared
@@ -90,7 +90,10 @@ __device__ __forceinline__ bool stream_wait(uint32_t bar, uint32_t parity, volat
 }
 
 // The producer: rows, tiles, 32-entry chunks of the row, segment pieces
-// placed in lane order into the open stage.
+// placed in lane order into the open stage.  Every piece is copied as its
+// 16-byte-aligned superset [a & ~3, (b + 3) & ~3) -- up to 3 elements of the
+// neighbouring segments on either side, which the stage's valid mask leaves
+// out -- so the producer never waits on segment data, only on the bounds.
 __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, const uint32_t* __restrict__ rows,
                                                uint32_t nrows, uint32_t* s_row) {
     const uint32_t lane = lane_id();
@@ -99,21 +102,18 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
     uint32_t s = 0, ph = 0;    // the stage to fill next and its phase parity
     uint32_t fill = 0;         // slots used in the open stage
     bool open = false;
-    uint32_t closed = 0;       // stages closed since the start (copies may be in flight in the last kStreamStages)
+    uint32_t closed = 0;       // stages closed since the start
     bool bad = false;
 
     auto acquire = [&]() -> bool {
         if (!stream_wait(smem_addr(&sm.empty[s]), ph ^ 1, abort)) return false;
-        // this stage's slots were last written by plain stores (head, tail,
-        // padding) as well as by copies: order those stores before the
-        // copies about to be issued into it
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        sm.mask[s][lane] = 0;  // kStreamCap / 32 == 32 words, one per lane
         fill = 0;
         open = true;
         return true;
     };
-    // Publishes the open stage (header, the slots written by plain stores)
-    // and arrives on its full barrier; the copies complete it.
+    // Publishes the open stage (header, valid mask) and arrives on its full
+    // barrier; the copies complete it.
     auto close = [&](uint32_t x, uint32_t lo, uint32_t flags) {
         if (lane == 0) sm.hdr[s] = StreamHdr{fill, x, lo, flags};
         __syncwarp();
@@ -134,13 +134,15 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
         if (ri >= nrows || bad) break;
         const uint32_t x = rows[ri];
         const uint32_t e0 = c.JR_R[x], e1 = c.JR_R[x + 1];
+        // the row's first 32 join values, kept across its tiles
+        const uint32_t y0 = e0 + lane < e1 ? ld_keep(&c.IC_R[e0 + lane], pol) : 0u;
         for (uint32_t t = 0; t < c.T && !bad; t++) {
             const uint32_t lo = t * c.tile_width;
             for (uint32_t eb = e0; eb < e1 && !bad; eb += 32) {
                 const uint32_t e = eb + lane;
                 uint32_t g0 = 0, g1 = 0;
                 if (e < e1) {
-                    const uint32_t y = ld_keep(&c.IC_R[e], pol);
+                    const uint32_t y = eb == e0 ? y0 : ld_keep(&c.IC_R[e], pol);
                     const uint64_t r = (uint64_t)y * c.T + t;
                     g0 = ld_keep(&c.JR_S[r], pol);
                     g1 = ld_keep(&c.JR_S[r + 1], pol);
@@ -155,40 +157,25 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
                     // aligned point kStreamPiece or fewer elements on
                     uint32_t b = g1;
                     if (g1 - a > kStreamPiece) b = (a + kStreamPiece) & ~3u;
-                    const uint32_t a4 = (a + 3) & ~3u, b4 = b & ~3u;
-                    const bool interior = a4 < b4;
-                    const uint32_t hn = interior ? a4 - a : b - a;  // head (or the whole piece if no interior)
-                    const uint32_t in = interior ? b4 - a4 : 0u;
-                    const uint32_t tn = interior ? b - b4 : 0u;
-                    const uint32_t need = a < g1 ? ((hn + 3) & ~3u) + in + ((tn + 3) & ~3u) : 0u;
+                    const uint32_t A0 = a & ~3u, A1 = (b + 3) & ~3u;
+                    const uint32_t need = a < g1 ? A1 - A0 : 0u;
                     const uint32_t incl = warp_incl_scan(need), excl = incl - need;
                     const uint32_t room = kStreamCap - fill;
-                    const bool place = need && incl <= room;  // lanes placed in order while they fit
                     const uint32_t fits = __ballot_sync(0xffffffffu, !need || incl <= room);
                     const uint32_t placed = fits == 0xffffffffu ? 32u : __ffs(~fits) - 1;  // lanes [0, placed)
-                    if (place && lane < placed) {
-                        uint32_t* zs = sm.z[s];
-                        uint32_t* vs = sm.v[s];
-                        uint32_t p = fill + excl;
-                        const uint32_t hslots = (hn + 3) & ~3u;
-                        for (uint32_t k = 0; k < hslots; k++) {
-                            const bool h = k < hn;
-                            zs[p + k] = h ? ld_keep(&c.IC_S[a + k], pol) : kEmpty32;
-                            vs[p + k] = h ? ld_keep(&c.VS[a + k], pol) : 0u;
-                        }
-                        p += hslots;
-                        if (in) {
-                            const uint32_t full = smem_addr(&sm.full[s]);
-                            mbar_expect_only(full, 8 * in);
-                            bulk_g2s(smem_addr(&zs[p]), &c.IC_S[a4], 4 * in, full, pol);
-                            bulk_g2s(smem_addr(&vs[p]), &c.VS[a4], 4 * in, full, pol);
-                            p += in;
-                        }
-                        const uint32_t tslots = (tn + 3) & ~3u;
-                        for (uint32_t k = 0; k < tslots; k++) {
-                            const bool h = k < tn;
-                            zs[p + k] = h ? ld_keep(&c.IC_S[b4 + k], pol) : kEmpty32;
-                            vs[p + k] = h ? ld_keep(&c.VS[b4 + k], pol) : 0u;
+                    if (need && lane < placed) {
+                        const uint32_t p = fill + excl;  // slot of element A0
+                        const uint32_t full = smem_addr(&sm.full[s]);
+                        mbar_expect_only(full, 8 * need);
+                        bulk_g2s(smem_addr(&sm.z[s][p]), &c.IC_S[A0], 4 * need, full, pol);
+                        bulk_g2s(smem_addr(&sm.v[s][p]), &c.VS[A0], 4 * need, full, pol);
+                        // valid slots [p + a - A0, p + b - A0)
+                        const uint32_t v0 = p + (a - A0), v1 = p + (b - A0);
+                        for (uint32_t w = v0 >> 5; w <= (v1 - 1) >> 5; w++) {
+                            const uint32_t lo_b = w * 32 > v0 ? 0u : v0 - w * 32;
+                            const uint32_t hi_b = w * 32 + 32 < v1 ? 32u : v1 - w * 32;
+                            const uint32_t bits = (hi_b == 32 ? 0xFFFFFFFFu : ((1u << hi_b) - 1u)) & ~((1u << lo_b) - 1u);
+                            atomicOr(&sm.mask[s][w], bits);
                         }
                         a = b;
                     }
@@ -271,7 +258,7 @@ __device__ __forceinline__ void stream_consume(const RowCtx& c, const Reserve& r
 #pragma unroll
             for (uint32_t u = 0; u < kUnroll; u++) {
                 const uint32_t i = base + u * 32 + lane;
-                const bool in = i < h.n;
+                const bool in = i < h.n && ((sm.mask[s][(base >> 5) + u] >> lane) & 1u);
                 z[u] = in ? zs[i] : kEmpty32;
                 v[u] = in ? vs[i] : 0u;
             }
