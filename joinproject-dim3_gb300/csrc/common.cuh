@@ -88,6 +88,11 @@ __device__ __forceinline__ uint32_t ld_keep(const uint32_t* a, uint64_t pol) {
     asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
     return v;
 }
+__device__ __forceinline__ uint2 ld_keep2(const uint2* a, uint64_t pol) {
+    uint2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(a), "l"(pol));
+    return v;
+}
 __device__ __forceinline__ void st_stream(uint2* a, uint2 v) { __stcs(a, v); }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }

@@ -644,10 +644,11 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cnt_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* cur_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* JR_S = ws_get<uint32_t>(c, nyt + 1);
-    // +4: the streamed bitmap rows copy 16-byte-aligned supersets of S
-    // segments, up to 3 elements past the last one
-    uint32_t* IC_S = ws_get<uint32_t>(c, nq + 4);
-    uint32_t* VS = ws_get<uint32_t>(c, nq + 4);
+    uint32_t* IC_S = ws_get<uint32_t>(c, nq);
+    uint32_t* VS = ws_get<uint32_t>(c, nq);
+    // +2: the streamed bitmap rows copy 16-byte-aligned supersets of S
+    // segments, up to one pair past the last one
+    uint2* ISV = ws_get<uint2>(c, nq + 2);
     uint32_t* Zq = ws_get<uint32_t>(c, nq);
     uint32_t* ucap = ws_get<uint32_t>(c, n);
     uint8_t* cls = ws_get<uint8_t>(c, n);
@@ -655,7 +656,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
     uint64_t* bsum2 = ws_get<uint64_t>(c, scan_storage((nyt > n ? nyt : n) + 1));
-    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !VS || !Zq || !ucap || !cls || !lists ||
+    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !VS || !ISV || !Zq || !ucap || !cls || !lists ||
         !cnt || !off || !bsum2)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
 
@@ -669,7 +670,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     k_scatter_r<<<grid_for(jp.nP, sm), 256, 0, st>>>(Pm, jp.nP, curx, IC_R);
     CHECK_LAUNCH();
     SCAN(U32Src{cnt_yt}, RowPtrDst{JR_S, cur_yt}, nyt + 1, bsum2, nullptr);
-    k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, Zq, nq, T, tile_shift, cur_yt, IC_S, VS);
+    k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, Zq, nq, T, tile_shift, cur_yt, IC_S, VS, ISV);
     CHECK_LAUNCH();
 
     RowCtx rc{};
@@ -678,6 +679,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     rc.JR_S = JR_S;
     rc.IC_S = IC_S;
     rc.VS = VS;
+    rc.ISV = ISV;
     rc.T = T;
     rc.tile_width = tile_width;
     rc.m = m;

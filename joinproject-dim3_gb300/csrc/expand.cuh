@@ -61,6 +61,7 @@ struct RowCtx {
     const uint32_t* JR_S;  // k*T+1 row pointers of S by (y id, z tile)
     const uint32_t* IC_S;  // z ids
     const uint32_t* VS;    // z values, parallel to IC_S (write pass)
+    const uint2* ISV;      // (z id, z value) pairs parallel to IC_S, or nullptr (value paths load one pair)
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
@@ -162,9 +163,24 @@ __device__ __forceinline__ Chunk load_chunk(const RowCtx& c, uint32_t eb, uint32
 // with a single memory latency.  Long segments: the lanes stride each
 // segment overlapping the piece, kUnroll x 32 candidates at a time, all
 // loads of a group issued first.
-template <class Set, class Sink>
-__device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, uint32_t p0, uint32_t p1, Set& set,
-                                             Sink& sink, uint64_t pol) {
+// One candidate's z id (and z value when the sink asks for values): a pair
+// load from ISV, or the id and value arrays.
+template <bool kPair, bool kValues>
+__device__ __forceinline__ void load_cand(const RowCtx& c, uint32_t j, bool act, uint64_t pol, uint32_t& z,
+                                          uint32_t& v) {
+    if (kPair && kValues) {
+        const uint2 p = act ? ld_keep2(&c.ISV[j], pol) : make_uint2(kEmpty32, 0u);
+        z = p.x;
+        v = p.y;
+    } else {
+        z = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
+        if (kValues) v = act ? ld_keep(&c.VS[j], pol) : 0u;
+    }
+}
+
+template <bool kPair, class Set, class Sink>
+__device__ __forceinline__ void expand_piece_impl(const RowCtx& c, const Chunk& ch, uint32_t p0, uint32_t p1,
+                                                  Set& set, Sink& sink, uint64_t pol) {
     const uint32_t lane = lane_id();
     const uint32_t nseg = __popc(__ballot_sync(0xffffffffu, ch.len != 0));
     if (ch.total < kFlatAvgMax * nseg) {
@@ -180,8 +196,7 @@ __device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, u
                 for (uint32_t step = 16; step >= 1; step >>= 1)
                     if (__shfl_sync(0xffffffffu, ch.incl, k + step - 1) <= ci) k += step;
                 const uint32_t j = __shfl_sync(0xffffffffu, ch.s0, k) + (ci - __shfl_sync(0xffffffffu, ch.excl, k));
-                z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
-                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
+                load_cand<kPair, Sink::kValues>(c, j, act, pol, z[u], v[u]);
             }
             uint32_t b[kUnroll];
 #pragma unroll
@@ -204,11 +219,7 @@ __device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, u
         for (; jb + 32 * kUnroll <= hi; jb += 32 * kUnroll) {
             uint32_t z[kUnroll], v[kUnroll];
 #pragma unroll
-            for (uint32_t u = 0; u < kUnroll; u++) {
-                const uint32_t j = ks0 + jb + u * 32 + lane;
-                z[u] = ld_keep(&c.IC_S[j], pol);
-                if (Sink::kValues) v[u] = ld_keep(&c.VS[j], pol);
-            }
+            for (uint32_t u = 0; u < kUnroll; u++) load_cand<kPair, Sink::kValues>(c, ks0 + jb + u * 32 + lane, true, pol, z[u], v[u]);
             uint32_t b[kUnroll];
 #pragma unroll
             for (uint32_t u = 0; u < kUnroll; u++) b[u] = __ballot_sync(0xffffffffu, set.insert(z[u], true));
@@ -222,9 +233,7 @@ __device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, u
 #pragma unroll
             for (uint32_t u = 0; u < kUnroll; u++) {
                 const uint32_t j = jb + u * 32 + lane;
-                const bool act = j < hi;
-                z[u] = act ? ld_keep(&c.IC_S[ks0 + j], pol) : kEmpty32;
-                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[ks0 + j], pol) : 0u;
+                load_cand<kPair, Sink::kValues>(c, ks0 + j, j < hi, pol, z[u], v[u]);
             }
             uint32_t b[kUnroll];
 #pragma unroll
@@ -233,6 +242,17 @@ __device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, u
             sink.take(b, v);
         }
     }
+}
+
+// Candidates [p0, p1) of a chunk: paired loads where the (z id, z value)
+// pairs exist and the sink takes values.
+template <class Set, class Sink>
+__device__ __forceinline__ void expand_piece(const RowCtx& c, const Chunk& ch, uint32_t p0, uint32_t p1, Set& set,
+                                             Sink& sink, uint64_t pol) {
+    if (Sink::kValues && c.ISV != nullptr)
+        expand_piece_impl<true>(c, ch, p0, p1, set, sink, pol);
+    else
+        expand_piece_impl<false>(c, ch, p0, p1, set, sink, pol);
 }
 
 // Warp-level expansion of the candidates of R entries [e0, e1) over S tiles

@@ -9,13 +9,13 @@
 // Here the CTA is split by role:
 //   producer (warp 0)  takes rows from the class's dynamic counter, reads the
 //                      row's S segment bounds for one tile 32 entries at a
-//                      time, and copies the segments' z ids and z values into
-//                      a ring of stages in shared memory: one cp.async.bulk
-//                      per array of the segment's 16-byte-aligned superset
-//                      (completion counted on the stage's mbarrier); a valid
-//                      mask per stage marks the segment's own slots.  A
-//                      segment longer than kStreamPiece is cut into pieces at
-//                      aligned points.
+//                      time, and copies the segments' (z id, z value) pairs
+//                      into a ring of stages in shared memory: one
+//                      cp.async.bulk of the segment's 16-byte-aligned
+//                      superset (completion counted on the stage's mbarrier);
+//                      a valid mask per stage marks the segment's own slots.
+//                      A segment longer than kStreamPiece is cut into pieces
+//                      at aligned points.
 //   consumers          every consumer warp takes an equal slice of each
 //                      stage: test-and-set of the tile bitmap from shared
 //                      memory, first insertions staged per warp and written
@@ -54,8 +54,7 @@ struct StreamHdr {
 // Dynamic shared memory of the kernel: the tile bitmap (bm_words, a
 // multiple of 4) then the fixed part below.
 struct StreamSmem {
-    uint32_t z[kStreamStages][kStreamCap];
-    uint32_t v[kStreamStages][kStreamCap];
+    uint2 zv[kStreamStages][kStreamCap];  // (z id, z value) per slot
     uint32_t stage[kStreamConsumers][kStreamStageVals];
     uint32_t mask[kStreamStages][kStreamCap / 32];  // valid slots of each stage
     StreamHdr hdr[kStreamStages];
@@ -90,17 +89,18 @@ __device__ __forceinline__ bool stream_wait(uint32_t bar, uint32_t parity, volat
 }
 
 // The producer: rows, tiles, 32-entry chunks of the row, segment pieces
-// placed in lane order into the open stage.  Every piece is copied as its
-// 16-byte-aligned superset [a & ~3, (b + 3) & ~3) -- up to 3 elements of the
-// neighbouring segments on either side, which the stage's valid mask leaves
-// out -- so the producer never waits on segment data, only on the bounds.
+// placed in lane order into the open stage.  Every piece is copied from the
+// (z id, z value) pairs as its 16-byte-aligned superset [a & ~1, (b + 1) & ~1)
+// -- at most one element of a neighbouring segment on either side, which the
+// stage's valid mask leaves out -- so the producer never waits on segment
+// data, only on the bounds.
 __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, const uint32_t* __restrict__ rows,
                                                uint32_t nrows, uint32_t* s_row) {
     const uint32_t lane = lane_id();
     const uint64_t pol = l2_keep_policy();
     volatile uint32_t* abort = &sm.abort;
     uint32_t s = 0, ph = 0;    // the stage to fill next and its phase parity
-    uint32_t fill = 0;         // slots used in the open stage
+    uint32_t fill = 0;         // slots used in the open stage (a multiple of 2)
     bool open = false;
     uint32_t closed = 0;       // stages closed since the start
     bool bad = false;
@@ -156,8 +156,8 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
                     // this lane's next piece [a, b): the segment's end, or an
                     // aligned point kStreamPiece or fewer elements on
                     uint32_t b = g1;
-                    if (g1 - a > kStreamPiece) b = (a + kStreamPiece) & ~3u;
-                    const uint32_t A0 = a & ~3u, A1 = (b + 3) & ~3u;
+                    if (g1 - a > kStreamPiece) b = (a + kStreamPiece) & ~1u;
+                    const uint32_t A0 = a & ~1u, A1 = (b + 1) & ~1u;
                     const uint32_t need = a < g1 ? A1 - A0 : 0u;
                     const uint32_t incl = warp_incl_scan(need), excl = incl - need;
                     const uint32_t room = kStreamCap - fill;
@@ -167,8 +167,7 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
                         const uint32_t p = fill + excl;  // slot of element A0
                         const uint32_t full = smem_addr(&sm.full[s]);
                         mbar_expect_only(full, 8 * need);
-                        bulk_g2s(smem_addr(&sm.z[s][p]), &c.IC_S[A0], 4 * need, full, pol);
-                        bulk_g2s(smem_addr(&sm.v[s][p]), &c.VS[A0], 4 * need, full, pol);
+                        bulk_g2s(smem_addr(&sm.zv[s][p]), &c.ISV[A0], 8 * need, full, pol);
                         // valid slots [p + a - A0, p + b - A0)
                         const uint32_t v0 = p + (a - A0), v1 = p + (b - A0);
                         for (uint32_t w = v0 >> 5; w <= (v1 - 1) >> 5; w++) {
@@ -250,8 +249,7 @@ __device__ __forceinline__ void stream_consume(const RowCtx& c, const Reserve& r
             cur_x = h.x;
             sink.xv = c.id2x[h.x];
         }
-        const uint32_t* zs = sm.z[s];
-        const uint32_t* vs = sm.v[s];
+        const uint2* zvs = sm.zv[s];
         const uint32_t base = cw * (kStreamCap / kStreamConsumers);
         if (base < h.n) {
             uint32_t z[kUnroll], v[kUnroll], b[kUnroll];
@@ -259,8 +257,9 @@ __device__ __forceinline__ void stream_consume(const RowCtx& c, const Reserve& r
             for (uint32_t u = 0; u < kUnroll; u++) {
                 const uint32_t i = base + u * 32 + lane;
                 const bool in = i < h.n && ((sm.mask[s][(base >> 5) + u] >> lane) & 1u);
-                z[u] = in ? zs[i] : kEmpty32;
-                v[u] = in ? vs[i] : 0u;
+                const uint2 p = in ? zvs[i] : make_uint2(kEmpty32, 0u);
+                z[u] = p.x;
+                v[u] = p.y;
             }
             TileBitmap set{bm, h.lo};
 #pragma unroll
