@@ -98,6 +98,7 @@ struct Params {
     uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
 };
 
+constexpr size_t kMaxSmemOptin = 227 * 1024;  // dynamic shared memory a CTA may opt into
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
 
 struct Scalars {
@@ -791,7 +792,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
                 list_m, dp.nd, dp.D, dp.Wd, dp.Wm, dp.cpr, dp.coff, id2x, id2z, out, nullptr, &sc->dense_base);
             CHECK_LAUNCH();
         }
-        if (c->prm.stream_rows) {
+        if (c->prm.stream_rows && stream_smem_bytes(bm_words) <= kMaxSmemOptin) {
             const size_t ss_s = stream_smem_bytes(bm_words);
             k_stream_bitmap<<<resident_grid(k_stream_bitmap, kStreamThreads, ss_s, sm), kStreamThreads, ss_s, st>>>(
                 rc, rs, L.m, L.n3, L.n4, bm_words);
@@ -1164,7 +1165,8 @@ int dim3g_create(int device, dim3g_ctx** out) {
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_stream_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)stream_smem_bytes(smem_m / 4)) == cudaSuccess &&
+                                   (int)(stream_smem_bytes(smem_m / 4) < kMaxSmemOptin ? stream_smem_bytes(smem_m / 4)
+                                                                                      : kMaxSmemOptin)) == cudaSuccess &&
               cudaFuncSetAttribute(k_dense_mma<kDenseBits>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kDenseSmem) == cudaSuccess &&
               cudaFuncSetAttribute(k_dense_mma<kDenseSumProject>, cudaFuncAttributeMaxDynamicSharedMemorySize,

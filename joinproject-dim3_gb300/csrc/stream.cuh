@@ -34,10 +34,17 @@
 
 namespace dim3g {
 
-constexpr uint32_t kStreamConsumers = 8;
+#ifndef DIM3G_STREAM_CONSUMERS
+#define DIM3G_STREAM_CONSUMERS 8
+#endif
+#ifndef DIM3G_STREAM_STAGES
+#define DIM3G_STREAM_STAGES 4
+#endif
+constexpr uint32_t kStreamConsumers = DIM3G_STREAM_CONSUMERS;
 constexpr uint32_t kStreamThreads = 32 * (kStreamConsumers + 1);
-constexpr uint32_t kStreamStages = 4;
-constexpr uint32_t kStreamCap = 1024;   // slots per stage: 128 per consumer warp (4 steps of 32)
+constexpr uint32_t kStreamStages = DIM3G_STREAM_STAGES;
+constexpr uint32_t kStreamCap = 128 * kStreamConsumers;  // slots per stage: 128 per consumer warp (4 steps of 32)
+static_assert(kStreamCap / kStreamConsumers == 32 * kUnroll, "a consumer's slice is one group of loads");
 constexpr uint32_t kStreamPiece = 496;  // longest piece of a segment placed at once (+ 6 alignment slots <= cap / 2)
 constexpr uint32_t kStreamStageVals = 256;  // staged z values per consumer warp
 constexpr unsigned long long kStreamWaitNs = 2000000000ull;
@@ -107,7 +114,7 @@ __device__ __forceinline__ void stream_produce(const RowCtx& c, StreamSmem& sm, 
 
     auto acquire = [&]() -> bool {
         if (!stream_wait(smem_addr(&sm.empty[s]), ph ^ 1, abort)) return false;
-        sm.mask[s][lane] = 0;  // kStreamCap / 32 == 32 words, one per lane
+        for (uint32_t w = lane; w < kStreamCap / 32; w += 32) sm.mask[s][w] = 0;
         fill = 0;
         open = true;
         return true;
