@@ -291,8 +291,13 @@ constexpr uint32_t kRowBlk = 1024;  // R entries staged at a time by the flatten
 struct CtaChunks {
     uint32_t n;              // deferred chunks (may exceed kBigCap: the rest ran at once)
     uint32_t eb[kBigCap];
-    uint32_t s0[kRowBlk];    // segment start of each staged entry
-    uint32_t incl[kRowBlk];  // flattened walk: inclusive prefix of the lengths; balanced walk: the lengths
+    union {
+        struct {
+            uint32_t s0[kRowBlk];    // segment start of each staged entry
+            uint32_t incl[kRowBlk];  // flattened walk: inclusive prefix of the lengths; balanced walk: the lengths
+        } seg;
+        uint32_t bnd[2 * kRowBlk];   // a row's entries' S row bounds over all z tiles (bitmap rows)
+    } st;
     uint32_t ctot[kRowBlk / 32];  // balanced walk: candidates of each staged 32-entry chunk
 };
 
@@ -344,8 +349,8 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
             const uint32_t i = tid * per + k;
             if (k < per && i < ne) {
                 run += len[k];
-                cc->s0[i] = s0[k];
-                cc->incl[i] = run;
+                cc->st.seg.s0[i] = s0[k];
+                cc->st.seg.incl[i] = run;
             }
         }
         const uint32_t total = sm_scan[nw];
@@ -363,11 +368,11 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
                 uint32_t lo = 0, hi = ne - 1;
                 while (lo < hi) {
                     const uint32_t mid = (lo + hi) >> 1;
-                    if (cc->incl[mid] > ci) hi = mid;
+                    if (cc->st.seg.incl[mid] > ci) hi = mid;
                     else lo = mid + 1;
                 }
-                const uint32_t excl = lo ? cc->incl[lo - 1] : 0u;
-                const uint32_t j = cc->s0[lo] + (ci - excl);
+                const uint32_t excl = lo ? cc->st.seg.incl[lo - 1] : 0u;
+                const uint32_t j = cc->st.seg.s0[lo] + (ci - excl);
                 z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
                 if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
             }
@@ -381,58 +386,75 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
     }
 }
 
-// Balanced CTA walk over R entries [e0, e1) and S tiles [t0, t1): the warps
-// stage kRowBlk entries' segments in shared memory, each warp loading whole
-// 32-entry chunks (every entry is loaded once), then every warp takes an
-// equal share of the block's candidates -- the chunks overlapping its share,
-// each through expand_piece with the chunk rebuilt from shared memory -- so
-// no warp idles at the next barrier while another expands a long chunk
-// alone.  Contains barriers; called by the whole CTA.
+// Balanced walk, staging half: the warps stage the segments of R entries
+// [eb, eb + ne) (ne <= kRowBlk) over S tiles [t0, t1) in shared memory, each
+// warp loading whole 32-entry chunks (every entry is loaded once), with each
+// chunk's candidate total.  No barrier; the expanding half follows one.
+__device__ __forceinline__ void balanced_stage(const RowCtx& c, uint32_t eb, uint32_t ne, uint32_t t0, uint32_t t1,
+                                               CtaChunks* cc, uint64_t pol) {
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nch = (ne + 31) >> 5;
+    for (uint32_t k = wib; k < nch; k += nw) {
+        const uint32_t i = k * 32 + lane, e = eb + i;
+        uint32_t s0 = 0, len = 0;
+        if (i < ne) {
+            const uint32_t y = ld_keep(&c.IC_R[e], pol);
+            const uint64_t r = (uint64_t)y * c.T;
+            s0 = ld_keep(&c.JR_S[r + t0], pol);
+            len = ld_keep(&c.JR_S[r + t1], pol) - s0;
+        }
+        cc->st.seg.s0[i] = s0;
+        cc->st.seg.incl[i] = len;
+        const uint32_t inc = warp_incl_scan(len);
+        if (__any_sync(0xffffffffu, inc < len)) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
+        if (lane == 31) cc->ctot[k] = inc;
+    }
+}
+
+// Balanced walk, expanding half: every warp takes an equal share of the
+// staged block's candidates -- the chunks overlapping its share, each through
+// expand_piece with the chunk rebuilt from shared memory -- so no warp idles
+// at the next barrier while another expands a long chunk alone.  No barrier.
+template <class Set, class Sink>
+__device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Set& set, Sink& sink, CtaChunks* cc,
+                                                uint64_t pol) {
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nch = (ne + 31) >> 5;
+    // prefix of the chunk totals (every warp computes it; nch <= 32)
+    const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
+    const uint32_t inc = warp_incl_scan(v);
+    if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
+    const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
+    // first chunk holding candidate p0: chunks with incl <= p0 form a prefix
+    for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
+        const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
+        const uint32_t cex = cin - ctot;
+        if (cex >= p1) break;
+        if (ctot == 0) continue;
+        Chunk ch;
+        ch.s0 = cc->st.seg.s0[k * 32 + lane];
+        ch.len = cc->st.seg.incl[k * 32 + lane];
+        ch.incl = warp_incl_scan(ch.len);
+        ch.excl = ch.incl - ch.len;
+        ch.total = ctot;
+        const uint32_t lo = p0 > cex ? p0 - cex : 0u, hi = p1 < cin ? p1 - cex : ctot;
+        expand_piece(c, ch, lo, hi, set, sink, pol);
+    }
+}
+
+// Balanced CTA walk over R entries [e0, e1) and S tiles [t0, t1), kRowBlk
+// entries at a time.  Contains barriers; called by the whole CTA.
 template <class Set, class Sink>
 __device__ __forceinline__ void cta_expand_balanced(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t t0,
                                                     uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint64_t pol = l2_keep_policy();
     for (uint32_t eb = e0; eb < e1; eb += kRowBlk) {
-        const uint32_t ne = min(kRowBlk, e1 - eb), nch = (ne + 31) >> 5;
-        for (uint32_t k = wib; k < nch; k += nw) {
-            const uint32_t i = k * 32 + lane, e = eb + i;
-            uint32_t s0 = 0, len = 0;
-            if (i < ne) {
-                const uint32_t y = ld_keep(&c.IC_R[e], pol);
-                const uint64_t r = (uint64_t)y * c.T;
-                s0 = ld_keep(&c.JR_S[r + t0], pol);
-                len = ld_keep(&c.JR_S[r + t1], pol) - s0;
-            }
-            cc->s0[i] = s0;
-            cc->incl[i] = len;
-            const uint32_t inc = warp_incl_scan(len);
-            if (__any_sync(0xffffffffu, inc < len)) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
-            if (lane == 31) cc->ctot[k] = inc;
-        }
+        const uint32_t ne = min(kRowBlk, e1 - eb);
+        balanced_stage(c, eb, ne, t0, t1, cc, pol);
         __syncthreads();
-        // prefix of the chunk totals (every warp computes it; nch <= 32)
-        const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
-        const uint32_t inc = warp_incl_scan(v);
-        if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
-        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-        const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
-        const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
-        // first chunk holding candidate p0: chunks with incl <= p0 form a prefix
-        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
-            const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
-            const uint32_t cex = cin - ctot;
-            if (cex >= p1) break;
-            if (ctot == 0) continue;
-            Chunk ch;
-            ch.s0 = cc->s0[k * 32 + lane];
-            ch.len = cc->incl[k * 32 + lane];
-            ch.incl = warp_incl_scan(ch.len);
-            ch.excl = ch.incl - ch.len;
-            ch.total = ctot;
-            const uint32_t lo = p0 > cex ? p0 - cex : 0u, hi = p1 < cin ? p1 - cex : ctot;
-            expand_piece(c, ch, lo, hi, set, sink, pol);
-        }
+        balanced_expand(c, ne, set, sink, cc, pol);
         __syncthreads();  // the staged table is rewritten by the next block
     }
 }

@@ -162,7 +162,8 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uin
 // Class 2: the whole CTA expands row x; a 2^block_lg-word table (hash set or
 // whole-domain bitmap) at smem, into each warp's sink (the caller sets its
 // x value and flushes it).  Called by all threads after a barrier that
-// follows the previous row.
+// follows the previous row; the caller's next call comes after another
+// barrier (the last warps may still be expanding when this returns).
 template <class Sink>
 __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, uint32_t* smem, Sink& sink,
                                                  uint32_t block_lg, CtaChunks* cc) {
@@ -176,6 +177,22 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
     const uint32_t n4 = (bm ? row_bitmap_words(c.m) : (1u << lg)) / 4;
     uint4* t4 = reinterpret_cast<uint4*>(smem);
     for (uint32_t s = threadIdx.x; s < n4; s += blockDim.x) t4[s] = make_uint4(fill, fill, fill, fill);
+    const uint32_t e0 = c.JR_R[x], ne = c.JR_R[x + 1] - e0;
+    if (c.cta_rr == 3 && ne <= kRowBlk) {
+        // balanced walk of one staging block: the table's clearing and the
+        // staging share one barrier; the caller's next-row barrier ends it
+        const uint64_t pol = l2_keep_policy();
+        balanced_stage(c, e0, ne, 0, c.T, cc, pol);
+        __syncthreads();
+        if (bm) {
+            TileBitmap set{smem, 0};
+            balanced_expand(c, ne, set, sink, cc, pol);
+        } else {
+            HashSet set{smem, lg, c.err};
+            balanced_expand(c, ne, set, sink, cc, pol);
+        }
+        return;
+    }
     __syncthreads();
     if (bm) {
         TileBitmap set{smem, 0};
@@ -183,6 +200,63 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
     } else {
         HashSet set{smem, lg, c.err};
         cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink, cc);
+    }
+}
+
+// Classes 3/4 with the balanced walk for a row of at most kRowBlk entries
+// whose S row bounds over all z tiles fit the staging table: the bounds
+// (T + 1 per entry) are read once for the row, so each tile's chunks come
+// from shared memory -- no global round trip and two barriers per tile.
+template <class Sink>
+__device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, uint32_t ne, uint32_t* bm,
+                                                  Sink& sink, CtaChunks* cc) {
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t T = c.T, TB = T + 1, nch = (ne + 31) >> 5;
+    const uint64_t pol = l2_keep_policy();
+    uint32_t* bnd = cc->st.bnd;
+    for (uint32_t i = threadIdx.x; i < ne; i += blockDim.x) {
+        const uint32_t y = ld_keep(&c.IC_R[e0 + i], pol);
+        const uint64_t r = (uint64_t)y * T;
+        for (uint32_t k = 0; k <= T; k++) bnd[i * TB + k] = ld_keep(&c.JR_S[r + k], pol);
+    }
+    for (uint32_t t = 0; t < T; t++) {
+        const uint32_t lo = t * c.tile_width;
+        const uint32_t width = min(c.tile_width, c.m - lo);
+        const uint32_t words4 = (((width + 31) >> 5) + 3) >> 2;
+        uint4* b4 = reinterpret_cast<uint4*>(bm);
+        for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
+        if (t == 0) __syncthreads();  // the staged bounds
+        for (uint32_t k = wib; k < nch; k += nw) {
+            const uint32_t i = k * 32 + lane;
+            const uint32_t len = i < ne ? bnd[i * TB + t + 1] - bnd[i * TB + t] : 0u;
+            const uint32_t inc = warp_incl_scan(len);
+            if (__any_sync(0xffffffffu, inc < len)) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
+            if (lane == 31) cc->ctot[k] = inc;
+        }
+        __syncthreads();  // the tile's bitmap cleared, its chunk totals written
+        const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
+        const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
+        TileBitmap set{bm, lo};
+        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
+            const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
+            const uint32_t cex = cin - ctot;
+            if (cex >= p1) break;
+            if (ctot == 0) continue;
+            const uint32_t i = k * 32 + lane;
+            Chunk ch;
+            ch.s0 = i < ne ? bnd[i * TB + t] : 0u;
+            ch.len = i < ne ? bnd[i * TB + t + 1] - ch.s0 : 0u;
+            ch.incl = warp_incl_scan(ch.len);
+            ch.excl = ch.incl - ch.len;
+            ch.total = ctot;
+            const uint32_t plo = p0 > cex ? p0 - cex : 0u, phi = p1 < cin ? p1 - cex : ctot;
+            expand_piece(c, ch, plo, phi, set, sink, pol);
+        }
+        __syncthreads();  // every insert into this tile done before the next clear
     }
 }
 
@@ -194,6 +268,13 @@ __device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, u
                                                   CtaChunks* cc) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
+    {
+        const uint32_t e0 = c.JR_R[x], ne = c.JR_R[x + 1] - e0;
+        if (c.cta_rr == 3 && ne <= kRowBlk && (uint64_t)ne * (c.T + 1) <= 2 * kRowBlk) {
+            bitmap_row_staged(c, e0, ne, bm, sink, cc);
+            return;
+        }
+    }
     for (uint32_t t = 0; t < c.T; t++) {
         const uint32_t lo = t * c.tile_width;
         const uint32_t width = min(c.tile_width, c.m - lo);
