@@ -32,6 +32,7 @@
 #include "scan.cuh"
 #include "single.cuh"
 #include "stream.cuh"
+#include "prefetch.cuh"
 
 using namespace dim3g;
 
@@ -96,6 +97,7 @@ struct Params {
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
     bool keep_roles = false;  // R drives the join whatever the sizes (no swap)
     uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
+    uint32_t prefetch_rows = 1;  // single pass, balanced walk: block-class rows fetched ahead (prefetch.cuh)
 };
 
 constexpr size_t kMaxSmemOptin = 227 * 1024;  // dynamic shared memory a CTA may opt into
@@ -803,8 +805,14 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[5], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[0], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
-        k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(rc, rs, L.b, L.nb,
-                                                                                          c->prm.block_lg);
+        if (c->prm.prefetch_rows && c->prm.cta_rr == 3) {
+            const size_t ss_p = (((size_t)1 << c->prm.block_lg) + (size_t)kPfWorkers * kStage) * 4;
+            k_single_block_pf<<<resident_grid(k_single_block_pf, kPfThreads, ss_p, sm), kPfThreads, ss_p, st>>>(
+                rc, rs, L.b, L.nb, c->prm.block_lg);
+        } else {
+            k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(rc, rs, L.b, L.nb,
+                                                                                              c->prm.block_lg);
+        }
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[6], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[1], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
@@ -1164,6 +1172,8 @@ int dim3g_create(int device, dim3g_ctx** out) {
                                    ((1 << 14) + 32 * (int)kStage) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_single_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    smem_m + 32 * (int)kStage * 4) == cudaSuccess &&
+              cudaFuncSetAttribute(k_single_block_pf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   ((1 << 14) + (int)(kPfWorkers * kStage)) * 4) == cudaSuccess &&
               cudaFuncSetAttribute(k_stream_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(stream_smem_bytes(smem_m / 4) < kMaxSmemOptin ? stream_smem_bytes(smem_m / 4)
                                                                                       : kMaxSmemOptin)) == cudaSuccess &&
@@ -1253,6 +1263,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "dense_mem_mb")) {
         if (v < 1 || v > (1 << 20)) return fail(c, DIM3G_ERR_INVALID, "dense_mem_mb must be in 1..2^20");
         c->prm.dense_mem = (uint64_t)v << 20;
+    } else if (!strcmp(name, "prefetch_rows")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "prefetch_rows must be 0 or 1");
+        c->prm.prefetch_rows = (uint32_t)v;
     } else if (!strcmp(name, "stream_rows")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "stream_rows must be 0 or 1");
         c->prm.stream_rows = (uint32_t)v;
@@ -1279,6 +1292,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "dense_mem_mb")) *v = (int64_t)(c->prm.dense_mem >> 20);
     else if (!strcmp(name, "keep_roles")) *v = c->prm.keep_roles ? 1 : 0;
     else if (!strcmp(name, "stream_rows")) *v = c->prm.stream_rows;
+    else if (!strcmp(name, "prefetch_rows")) *v = c->prm.prefetch_rows;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

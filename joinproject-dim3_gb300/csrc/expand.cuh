@@ -390,9 +390,10 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
 // [eb, eb + ne) (ne <= kRowBlk) over S tiles [t0, t1) in shared memory, each
 // warp loading whole 32-entry chunks (every entry is loaded once), with each
 // chunk's candidate total.  No barrier; the expanding half follows one.
+// (wib, nw): this warp's index among the nw warps that share the work.
 __device__ __forceinline__ void balanced_stage(const RowCtx& c, uint32_t eb, uint32_t ne, uint32_t t0, uint32_t t1,
-                                               CtaChunks* cc, uint64_t pol) {
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+                                               CtaChunks* cc, uint64_t pol, uint32_t wib, uint32_t nw) {
+    const uint32_t lane = lane_id();
     const uint32_t nch = (ne + 31) >> 5;
     for (uint32_t k = wib; k < nch; k += nw) {
         const uint32_t i = k * 32 + lane, e = eb + i;
@@ -415,13 +416,16 @@ __device__ __forceinline__ void balanced_stage(const RowCtx& c, uint32_t eb, uin
 // staged block's candidates -- the chunks overlapping its share, each through
 // expand_piece with the chunk rebuilt from shared memory -- so no warp idles
 // at the next barrier while another expands a long chunk alone.  No barrier.
+// s0 / len / ctot: the staged segment starts and lengths and the chunk
+// totals (a CtaChunks' arrays, or a prefetched row's).
 template <class Set, class Sink>
-__device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Set& set, Sink& sink, CtaChunks* cc,
-                                                uint64_t pol) {
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Set& set, Sink& sink,
+                                                const uint32_t* s0a, const uint32_t* lena, const uint32_t* ctota,
+                                                uint64_t pol, uint32_t wib, uint32_t nw) {
+    const uint32_t lane = lane_id();
     const uint32_t nch = (ne + 31) >> 5;
     // prefix of the chunk totals (every warp computes it; nch <= 32)
-    const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
+    const uint32_t v = lane < nch ? ctota[lane] : 0u;
     const uint32_t inc = warp_incl_scan(v);
     if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
@@ -434,8 +438,8 @@ __device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Se
         if (cex >= p1) break;
         if (ctot == 0) continue;
         Chunk ch;
-        ch.s0 = cc->st.seg.s0[k * 32 + lane];
-        ch.len = cc->st.seg.incl[k * 32 + lane];
+        ch.s0 = s0a[k * 32 + lane];
+        ch.len = lena[k * 32 + lane];
         ch.incl = warp_incl_scan(ch.len);
         ch.excl = ch.incl - ch.len;
         ch.total = ctot;
@@ -450,11 +454,12 @@ template <class Set, class Sink>
 __device__ __forceinline__ void cta_expand_balanced(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t t0,
                                                     uint32_t t1, Set& set, Sink& sink, CtaChunks* cc) {
     const uint64_t pol = l2_keep_policy();
+    const uint32_t wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (uint32_t eb = e0; eb < e1; eb += kRowBlk) {
         const uint32_t ne = min(kRowBlk, e1 - eb);
-        balanced_stage(c, eb, ne, t0, t1, cc, pol);
+        balanced_stage(c, eb, ne, t0, t1, cc, pol, wib, nw);
         __syncthreads();
-        balanced_expand(c, ne, set, sink, cc, pol);
+        balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw);
         __syncthreads();  // the staged table is rewritten by the next block
     }
 }

@@ -182,14 +182,15 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
         // balanced walk of one staging block: the table's clearing and the
         // staging share one barrier; the caller's next-row barrier ends it
         const uint64_t pol = l2_keep_policy();
-        balanced_stage(c, e0, ne, 0, c.T, cc, pol);
+        const uint32_t nw = blockDim.x >> 5;
+        balanced_stage(c, e0, ne, 0, c.T, cc, pol, wib, nw);
         __syncthreads();
         if (bm) {
             TileBitmap set{smem, 0};
-            balanced_expand(c, ne, set, sink, cc, pol);
+            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw);
         } else {
             HashSet set{smem, lg, c.err};
-            balanced_expand(c, ne, set, sink, cc, pol);
+            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw);
         }
         return;
     }

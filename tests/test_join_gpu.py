@@ -181,6 +181,33 @@ def test_streamed_bitmap_rows_agree(built, golden, params):
     c.close()
 
 
+@pytest.mark.parametrize("prefetch", [1, 0])
+def test_prefetched_block_rows_agree(built, golden, prefetch):
+    """Block-class rows with their metadata fetched ahead by a producer warp
+    (prefetch_rows = 1) or not: exact on the golden cases with most rows in
+    the block class (small warp sets), on rows of more than 64 join values
+    (staged by the expanding warps) and on a row of 3000 join values (staged
+    in blocks of 1024), against the oracle."""
+    import dim3gpu
+    from oracle import oracle_py as O
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    for k, v in (("prefetch_rows", prefetch), ("warp_slots_log2", 6), ("block_slots_log2", 14)):
+        c.set_param(k, v)
+    for name in ["grd_small", "grd_all_dense", "grd_dense_z", "chung_lu_s005", "zipf_1m_s001", "one_join_value"]:
+        R, S = case_inputs(name, index, arrays)
+        check_pairs(c.join_project(R, S), index[name], arrays, name)
+    rng = np.random.default_rng(11)
+    R = np.stack([np.zeros(3000, np.uint32), np.arange(3000, dtype=np.uint32)], 1)
+    R = np.concatenate([R, rng.integers(1, 50, size=(2000, 2)).astype(np.uint32)])
+    S = np.stack([rng.integers(0, 6000, 5000), rng.integers(0, 3000, 5000)], 1).astype(np.uint32)
+    want, n, h, _ = O.join_project(R, S)
+    got = c.join_project(R, S)
+    assert got.shape[0] == n and O.set_hash(got) == h
+    assert np.array_equal(O.sorted_pairs(got), O.sorted_pairs(want))
+    c.close()
+
+
 def test_repeated_calls_are_stable(ctx, golden):
     index, arrays = golden
     R, S = case_inputs("chung_lu_s005", index, arrays)
