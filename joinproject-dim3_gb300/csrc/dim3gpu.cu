@@ -97,7 +97,7 @@ struct Params {
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
     bool keep_roles = false;  // R drives the join whatever the sizes (no swap)
     uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
-    uint32_t prefetch_rows = 1;  // single pass, balanced walk: block-class rows fetched ahead (prefetch.cuh)
+    uint32_t prefetch_rows = 0;  // single pass, balanced walk: block-class rows fetched ahead (prefetch.cuh)
 };
 
 constexpr size_t kMaxSmemOptin = 227 * 1024;  // dynamic shared memory a CTA may opt into
@@ -727,7 +727,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     const size_t smem_b = (size_t)1 << c->prm.block_lg << 2;
     size_t smem_m = (size_t)((((tile_width + 31) / 32) + 3) / 4) * 16;  // whole uint4 words (cleared as uint4)
     if (smem_m < 128) smem_m = 128;  // idle lanes touch words 0..31
-    const int blk_m = tile_width > (1u << 19) ? 1024 : 512;
+    const int blk_m = tile_width > (1u << 19) ? 1024 : DIM3G_BM_THREADS;
     const unsigned g_w = resident_grid(k_rows_warp<true>, 32 * wpc, smem_w, sm);
     const int blk_b = (int)c->prm.block_threads;
     const unsigned g_b = resident_grid(k_rows_block<true>, blk_b, smem_b, sm);

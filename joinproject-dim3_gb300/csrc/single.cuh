@@ -331,8 +331,18 @@ static __global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve 
 }
 
 // Classes 3/4: one CTA per row; a bitmap of bitmap_words, then one staging
-// buffer per warp.
-static __global__ void __launch_bounds__(1024) k_single_bitmap(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
+// buffer per warp.  DIM3G_BM_THREADS threads a CTA for tiles of up to 2^19
+// z ids (1024 for wider tiles).
+#ifndef DIM3G_BM_THREADS
+#define DIM3G_BM_THREADS 512
+#endif
+#ifndef DIM3G_BM_BOUNDS
+#define DIM3G_BM_BOUNDS 1024
+#endif
+#ifndef DIM3G_BM_MINB
+#define DIM3G_BM_MINB 1
+#endif
+static __global__ void __launch_bounds__(DIM3G_BM_BOUNDS, DIM3G_BM_MINB) k_single_bitmap(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
                                                                const unsigned long long* __restrict__ n3,
                                                                const unsigned long long* __restrict__ n4,
                                                                uint32_t bitmap_words) {
