@@ -66,6 +66,9 @@ typedef struct {
                                   too little heavy work, 3 no budget, 4 cost model, 5 a multiplicity above 16
                                   (summaries), 6 light buckets too large (summaries) */
     uint32_t dense_bucket_max; /* largest per-tile light bucket (summaries) */
+    uint64_t table_slots;      /* slots of the three mapping hash tables (sized by a distinct-key sketch) */
+    uint32_t table_rebuilds;   /* 1 when the sketch-sized tables overfilled and the mapping ran again at full size */
+    uint32_t pad0;
 } dim3g_stats;
 
 /* ---- context ------------------------------------------------------- */
@@ -92,6 +95,15 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * "dense_k_max" (32..4096: most join values in that product),
  * "dense_mem_mb" (bitmap budget of that product, default 16384: it takes as
  * many heavy rows as their x z bitmap fits, the largest first),
+ * "sized_tables" (1: the mapping's hash tables are sized by a distinct-key
+ * sketch to fit the L2 where keys repeat; 0: by the tuple counts),
+ * "table_slack_pct" (5..1000, default 150: slots of a sketch-sized table per
+ * estimated distinct key, in percent; a table that overfills is rebuilt at
+ * full size),
+ * "stream_rows" (1: bitmap-class rows of the single pass streamed into shared
+ * memory by bulk copies -- exact, measured slower on the 2-hop),
+ * "prefetch_rows" (1: block-class rows of the single pass fetched ahead by a
+ * producer warp -- exact, measured slower on the 2-hop),
  * "keep_roles" (0: the larger relation drives the join, the reference's
  * swap at dim3.hpp:993-994, so a smaller R yields (S.first, R.first) pairs;
  * 1: R always drives and pairs are always (R.first, S.first) -- for joining

@@ -96,6 +96,8 @@ struct Params {
     uint32_t dense_k_max = 2048;  // most join values in the dense product
     uint64_t dense_mem = (uint64_t)16 << 30;  // bitmap bytes of the dense block
     bool keep_roles = false;  // R drives the join whatever the sizes (no swap)
+    bool sized_tables = true;  // mapping tables sized by a distinct-key sketch (mapping.cuh)
+    uint32_t table_slack_pct = 150;  // sketch-sized table slots per estimated distinct key, percent
     uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
     uint32_t prefetch_rows = 0;  // single pass, balanced walk: block-class rows fetched ahead (prefetch.cuh)
 };
@@ -585,34 +587,76 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     CU(cudaEventRecord(c->ev[0], st));
 
     Scalars* sc = ws_get<Scalars>(c, 1);
-    const uint64_t capP = next_pow2(jp.nP * 2 < 1024 ? 1024 : jp.nP * 2);
-    const uint64_t capQ = next_pow2(jp.nQ * 2 < 1024 ? 1024 : jp.nQ * 2);
-    DevTable tx{ws_get<unsigned long long>(c, capP), capP - 1};
-    DevTable ty{ws_get<unsigned long long>(c, capP), capP - 1};
-    DevTable tz{ws_get<unsigned long long>(c, capQ), capQ - 1};
+    const uint64_t fullP = next_pow2(jp.nP * 2 < 1024 ? 1024 : jp.nP * 2);
+    const uint64_t fullQ = next_pow2(jp.nQ * 2 < 1024 ? 1024 : jp.nQ * 2);
     uint2* Qk = ws_get<uint2>(c, jp.nQ);
     uint2* Pm = ws_get<uint2>(c, jp.nP);
     uint32_t* id2x = ws_get<uint32_t>(c, jp.nP);
     uint32_t* id2z = ws_get<uint32_t>(c, round_up(jp.nQ, 1024) + 1024);  // whole 1024-id chunks (dense emission)
-    uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(capP > capQ ? capP : capQ));
-    if (!sc || !tx.slots || !ty.slots || !tz.slots || !Qk || !Pm || !id2x || !id2z || !bsum)
-        return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
+    uint32_t* regs = ws_get<uint32_t>(c, 3 * kSketchRegs);
+    if (!sc || !Qk || !Pm || !id2x || !id2z || !regs) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
 
-    CU(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
-    CU(cudaMemsetAsync(tx.slots, 0xff, capP * 8, st));
-    CU(cudaMemsetAsync(ty.slots, 0xff, capP * 8, st));
-    CU(cudaMemsetAsync(tz.slots, 0xff, capQ * 8, st));
+    // table capacities from the distinct-key sketch (see mapping.cuh)
+    uint64_t capX = fullP, capY = fullP, capZ = fullQ;
+    if (c->prm.sized_tables) {
+        CU(cudaMemsetAsync(regs, 0, 3 * kSketchRegs * 4, st));
+        k_sketch<<<grid_for(jp.nP > jp.nQ ? jp.nP : jp.nQ, sm, 2), 256, 0, st>>>(jp.P, jp.nP, jp.Q, jp.nQ, regs);
+        CHECK_LAUNCH();
+        std::vector<uint32_t> hr(3 * kSketchRegs);
+        CU(cudaMemcpyAsync(hr.data(), regs, 3 * kSketchRegs * 4, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        auto sized = [&](const uint32_t* r, uint64_t full) {
+            double sum = 0;
+            uint32_t zeros = 0;
+            for (uint32_t k = 0; k < kSketchRegs; k++) {
+                sum += ldexp(1.0, -(int)r[k]);
+                zeros += r[k] == 0;
+            }
+            const double M = kSketchRegs;
+            double e = 0.7213 / (1.0 + 1.079 / M) * M * M / sum;
+            if (e <= 2.5 * M && zeros) e = M * log(M / zeros);  // small-range estimate
+            const uint64_t cap = next_pow2((uint64_t)(c->prm.table_slack_pct / 100.0 * e) + 1024);
+            return cap < full ? cap : full;
+        };
+        capX = sized(hr.data(), fullP);
+        capY = sized(hr.data() + kSketchRegs, fullP);
+        capZ = sized(hr.data() + 2 * kSketchRegs, fullQ);
+    }
+    DevTable tx{}, ty{}, tz{};
+    for (int attempt = 0;; attempt++) {
+        const bool sized = capX < fullP || capY < fullP || capZ < fullQ;
+        const uint64_t lim = sized ? kSizedProbeLimit : 0;
+        tx = DevTable{ws_get<unsigned long long>(c, capX), capX - 1, lim};
+        ty = DevTable{ws_get<unsigned long long>(c, capY), capY - 1, lim};
+        tz = DevTable{ws_get<unsigned long long>(c, capZ), capZ - 1, lim};
+        const uint64_t capM = capX > capY ? (capX > capZ ? capX : capZ) : (capY > capZ ? capY : capZ);
+        uint64_t* bsum = ws_get<uint64_t>(c, scan_storage(capM));
+        if (!tx.slots || !ty.slots || !tz.slots || !bsum) return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (mapping)");
+        CU(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
+        CU(cudaMemsetAsync(tx.slots, 0xff, capX * 8, st));
+        CU(cudaMemsetAsync(ty.slots, 0xff, capY * 8, st));
+        CU(cudaMemsetAsync(tz.slots, 0xff, capZ * 8, st));
 
-    k_insert_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, &sc->err);
-    CHECK_LAUNCH();
-    SCAN(OccupiedSrc{ty.slots}, AssignIdDst{ty.slots, nullptr}, capP, bsum, &sc->ny);
-    SCAN(OccupiedSrc{tx.slots}, AssignIdDst{tx.slots, id2x}, capP, bsum, &sc->nx);
-    k_probe_q<<<grid_for(jp.nQ, sm), 256, 0, st>>>(jp.Q, jp.nQ, ty, tz, Qk, &sc->nkept, &sc->err);
-    CHECK_LAUNCH();
-    SCAN(OccupiedSrc{tz.slots}, AssignIdDst{tz.slots, id2z}, capQ, bsum, &sc->nz);
-    CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-    CU(cudaStreamSynchronize(st));
+        k_insert_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, &sc->err);
+        CHECK_LAUNCH();
+        SCAN(OccupiedSrc{ty.slots}, AssignIdDst{ty.slots, nullptr}, capY, bsum, &sc->ny);
+        SCAN(OccupiedSrc{tx.slots}, AssignIdDst{tx.slots, id2x}, capX, bsum, &sc->nx);
+        k_probe_q<<<grid_for(jp.nQ, sm), 256, 0, st>>>(jp.Q, jp.nQ, ty, tz, Qk, &sc->nkept, &sc->err);
+        CHECK_LAUNCH();
+        SCAN(OccupiedSrc{tz.slots}, AssignIdDst{tz.slots, id2z}, capZ, bsum, &sc->nz);
+        CU(cudaMemcpyAsync(c->h_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        if (sized && attempt == 0 && c->h_sc->err == kErrProbeLimit) {
+            // a table fuller than the sketch said: build again at full size
+            capX = capY = fullP;
+            capZ = fullQ;
+            S.table_rebuilds++;
+            continue;
+        }
+        break;
+    }
     if (c->h_sc->err) return fail(c, DIM3G_ERR_DEVICE, "device bound violated in mapping (flags %u)", c->h_sc->err);
+    S.table_slots = capX + capY + capZ;
     const uint32_t n = (uint32_t)c->h_sc->nx, k = (uint32_t)c->h_sc->ny, m = (uint32_t)c->h_sc->nz;
     const uint64_t nq = c->h_sc->nkept;
     S.nx = n;
@@ -1263,6 +1307,12 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "dense_mem_mb")) {
         if (v < 1 || v > (1 << 20)) return fail(c, DIM3G_ERR_INVALID, "dense_mem_mb must be in 1..2^20");
         c->prm.dense_mem = (uint64_t)v << 20;
+    } else if (!strcmp(name, "sized_tables")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "sized_tables must be 0 or 1");
+        c->prm.sized_tables = v == 1;
+    } else if (!strcmp(name, "table_slack_pct")) {
+        if (v < 5 || v > 1000) return fail(c, DIM3G_ERR_INVALID, "table_slack_pct must be in 5..1000");
+        c->prm.table_slack_pct = (uint32_t)v;
     } else if (!strcmp(name, "prefetch_rows")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "prefetch_rows must be 0 or 1");
         c->prm.prefetch_rows = (uint32_t)v;
@@ -1293,6 +1343,8 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "keep_roles")) *v = c->prm.keep_roles ? 1 : 0;
     else if (!strcmp(name, "stream_rows")) *v = c->prm.stream_rows;
     else if (!strcmp(name, "prefetch_rows")) *v = c->prm.prefetch_rows;
+    else if (!strcmp(name, "sized_tables")) *v = c->prm.sized_tables ? 1 : 0;
+    else if (!strcmp(name, "table_slack_pct")) *v = c->prm.table_slack_pct;
     else return DIM3G_ERR_INVALID;
     return DIM3G_OK;
 }

@@ -48,6 +48,7 @@ class Stats(ctypes.Structure):
         ("out_j_cls", ctypes.c_uint64 * 3), ("n_out_cls", ctypes.c_uint64 * 3),
         ("ms_dense", ctypes.c_float * 3), ("dense_kp", ctypes.c_uint32),
         ("dense_light", ctypes.c_uint64), ("dense_skip", ctypes.c_uint32), ("dense_bucket_max", ctypes.c_uint32),
+        ("table_slots", ctypes.c_uint64), ("table_rebuilds", ctypes.c_uint32), ("pad0", ctypes.c_uint32),
     ]
 
     def as_dict(self):

@@ -208,6 +208,31 @@ def test_prefetched_block_rows_agree(built, golden, prefetch):
     c.close()
 
 
+@pytest.mark.parametrize("sized,slack", [(1, 150), (0, 150), (1, 10)])
+def test_mapping_tables_sized_by_sketch(built, golden, sized, slack):
+    """The mapping's hash tables sized by the distinct-key sketch (far
+    smaller than tuple-sized ones where keys repeat), tuple-sized, and sized
+    too small on purpose (10 % of the distinct keys): the overfilled build is
+    detected and redone at full size.  All exact."""
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    c.set_param("sized_tables", sized)
+    c.set_param("table_slack_pct", slack)
+    for name in ["chung_lu_s005", "grd_sparse", "zipf_1m_s001", "heavy_duplicates", "extreme_keys", "grd_classical"]:
+        R, S = case_inputs(name, index, arrays)
+        check_pairs(c.join_project(R, S), index[name], arrays, name)
+        p, cnt = c.join_count(R, S)
+        check_groups(p, cnt, index[name], arrays, name)
+        st = c.stats()
+        full = 2 * (1 << int(np.ceil(np.log2(max(1024, 2 * max(R.shape[0], S.shape[0]))))))
+        if sized and slack == 10 and st["nx"] > 2000:
+            assert st["table_rebuilds"] == 1, (name, st["table_slots"])
+        if sized and slack == 150 and name == "chung_lu_s005":
+            assert st["table_rebuilds"] == 0 and st["table_slots"] < full, (st["table_slots"], full)
+    c.close()
+
+
 def test_repeated_calls_are_stable(ctx, golden):
     index, arrays = golden
     R, S = case_inputs("chung_lu_s005", index, arrays)
