@@ -343,7 +343,8 @@ int dim3g_tuning_key(dim3g_ctx* ctx, const uint32_t* d_R, uint64_t nR, const uin
  * defaults, which were measured once on a GB300): the tcgen05 fp8 product's
  * throughput on all-ones operands at K = 4096 (fp8_tflops: the ceiling of
  * k_dense_mma, dense flops 2 M N K per second), its fixed time per 128 x 256
- * tile at K = 128 (tile_us: TMA fill and epilogue), and a device-to-device
+ * tile at K = 128 (tile_us: TMA fill and epilogue; the difference between
+ * grids of 16 and of 8 tiles per SM, so launch costs cancel), and a device-to-device
  * copy's bandwidth (hbm_gbs, read + write bytes).  Allocates about 100 MB of
  * workspace; a few ms. */
 typedef struct {

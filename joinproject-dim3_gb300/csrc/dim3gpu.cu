@@ -692,7 +692,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cur_yt = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* JR_S = ws_get<uint32_t>(c, nyt + 1);
     uint32_t* IC_S = ws_get<uint32_t>(c, nq);
-    uint32_t* VS = ws_get<uint32_t>(c, nq);
+    uint32_t* VS = nullptr;  // the value paths read the pairs in ISV
     // +2: the streamed bitmap rows copy 16-byte-aligned supersets of S
     // segments, up to one pair past the last one
     uint2* ISV = ws_get<uint2>(c, nq + 2);
@@ -703,7 +703,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
     uint64_t* bsum2 = ws_get<uint64_t>(c, scan_storage((nyt > n ? nyt : n) + 1));
-    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !VS || !ISV || !Zq || !ucap || !cls || !lists ||
+    if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !ISV || !Zq || !ucap || !cls || !lists ||
         !cnt || !off || !bsum2)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
 
@@ -1464,10 +1464,12 @@ int dim3g_join_count_summary(dim3g_ctx* c, const uint32_t* dR, uint64_t nR, cons
     return run_summary(c, dR, nR, dS, nS, true, tiles, tile_lo, tile_hi, out);
 }
 
-// The product kernel of the dense block on all-ones operands: a grid of
-// 8 tiles per SM of 128 x 256, at K = 4096 (the MMA rate) and at K = 128
-// (the fixed time of a tile), each the best of 5 launches timed with events
-// on the context's stream; then a device-to-device copy of 512 MB.
+// The product kernel of the dense block on all-ones operands, timed with
+// events on the context's stream (best of 5 launches after one warm-up): at
+// K = 4096 over 8 tiles of 128 x 256 per SM (the MMA rate), and at K = 128
+// over 8 and over 16 tiles per SM (a tile's fixed time: the difference
+// divided by 8, so the launch's own fixed costs cancel); then a
+// device-to-device copy of 512 MB.
 int dim3g_calibrate(dim3g_ctx* c, dim3g_calibration* out) {
     if (!c || !out) return DIM3G_ERR_INVALID;
     memset(out, 0, sizeof *out);
@@ -1476,11 +1478,11 @@ int dim3g_calibrate(dim3g_ctx* c, dim3g_calibration* out) {
     cudaStream_t st = c->stream;
     const int sm = c->sm_count;
     const uint32_t nt = 16, mt = (uint32_t)(8 * sm + nt - 1) / nt;  // >= 8 tiles per SM
-    const uint64_t Mp = (uint64_t)mt * kDenseBM, Np = (uint64_t)nt * kDenseBN, Wd = Np / 32;
+    const uint64_t Mp = (uint64_t)mt * kDenseBM, Np = (uint64_t)nt * kDenseBN;
     const uint32_t kmax = 4096;
     uint8_t* A = ws_get<uint8_t>(c, Mp * kmax);
-    uint8_t* B = ws_get<uint8_t>(c, Np * kmax);
-    uint32_t* D = ws_get<uint32_t>(c, Mp * Wd);
+    uint8_t* B = ws_get<uint8_t>(c, Np * kmax);  // also 2 Np rows of 128 bytes
+    uint32_t* D = ws_get<uint32_t>(c, Mp * (2 * Np / 32));
     unsigned int* err = ws_get<unsigned int>(c, 1);
     const size_t copy_bytes = (size_t)512 << 20;
     char* src = ws_get<char>(c, copy_bytes);
@@ -1490,18 +1492,20 @@ int dim3g_calibrate(dim3g_ctx* c, dim3g_calibration* out) {
     CU(cudaMemsetAsync(B, kFp8One, Np * kmax, st));
     CU(cudaMemsetAsync(err, 0, 4, st));
     CU(cudaMemsetAsync(src, 1, copy_bytes, st));
-    const uint32_t kps[2] = {kmax, kDenseBK};
-    float best[2] = {1e30f, 1e30f};
-    const unsigned grid = (unsigned)((uint64_t)mt * nt < (uint64_t)sm ? (uint64_t)mt * nt : (uint64_t)sm);
-    for (int which = 0; which < 2; which++) {
-        const uint32_t Kp = kps[which];
+    // runs: {K, column tiles}
+    const uint32_t kps[3] = {kmax, kDenseBK, kDenseBK}, nts[3] = {nt, nt, 2 * nt};
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    for (int which = 0; which < 3; which++) {
+        const uint32_t Kp = kps[which], ntw = nts[which];
+        const uint64_t Npw = (uint64_t)ntw * kDenseBN, Wd = Npw / 32;
+        const unsigned grid = (unsigned)((uint64_t)mt * ntw < (uint64_t)sm ? (uint64_t)mt * ntw : (uint64_t)sm);
         CUtensorMap mA, mB;
         int r = dense_map(c, &mA, A, Mp, Kp, kDenseBM);
-        if (!r) r = dense_map(c, &mB, B, Np, Kp, kDenseBN);
+        if (!r) r = dense_map(c, &mB, B, Npw, Kp, kDenseBN);
         if (r) return r;
         for (int rep = 0; rep < 6; rep++) {  // the first launch warms up
             CU(cudaEventRecord(c->evd[0], st));
-            k_dense_mma<kDenseBits><<<grid, kDenseThreads, kDenseSmem, st>>>(mA, mB, D, (uint32_t)Wd, mt, nt,
+            k_dense_mma<kDenseBits><<<grid, kDenseThreads, kDenseSmem, st>>>(mA, mB, D, (uint32_t)Wd, mt, ntw,
                                                                               Kp / kDenseBK, err, DenseSum{});
             CHECK_LAUNCH();
             CU(cudaEventRecord(c->evd[1], st));
@@ -1524,13 +1528,15 @@ int dim3g_calibrate(dim3g_ctx* c, dim3g_calibration* out) {
     unsigned int h_err = 0;
     CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
     if (h_err) return fail(c, DIM3G_ERR_DEVICE, "calibration product reported flags %u", h_err);
-    const double tiles_per_sm = ceil((double)mt * nt / grid);
+    const unsigned grid0 = (unsigned)((uint64_t)mt * nt < (uint64_t)sm ? (uint64_t)mt * nt : (uint64_t)sm);
+    const double tiles_per_sm = ceil((double)mt * nt / grid0);
     const double flops = 2.0 * (double)Mp * (double)Np * kmax;
+    const double tile_s = (best[2] > best[1] ? best[2] - best[1] : best[1]) * 1e-3 / tiles_per_sm;
     out->fp8_tflops = (float)(flops / (best[0] * 1e-3) / 1e12);
-    out->tile_us = (float)(best[1] * 1e3 / tiles_per_sm);
+    out->tile_us = (float)(tile_s * 1e6);
     out->hbm_gbs = (float)(2.0 * copy_bytes / (copy_ms * 1e-3) / 1e9);
-    c->cm.sm_flops = flops / (best[0] * 1e-3) / grid;
-    c->cm.tile_s = best[1] * 1e-3 / tiles_per_sm;
+    c->cm.sm_flops = flops / (best[0] * 1e-3) / grid0;
+    c->cm.tile_s = tile_s;
     c->cm.dense_bw = 2.0 * copy_bytes / (copy_ms * 1e-3);
     c->cm.calibrated = true;
     out->sparse_gbs = (float)(c->cm.sparse_bw / 1e9);

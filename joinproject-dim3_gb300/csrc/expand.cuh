@@ -60,7 +60,7 @@ struct RowCtx {
     const uint32_t* IC_R;  // y ids
     const uint32_t* JR_S;  // k*T+1 row pointers of S by (y id, z tile)
     const uint32_t* IC_S;  // z ids
-    const uint32_t* VS;    // z values, parallel to IC_S (write pass)
+    const uint32_t* VS;    // z values, parallel to IC_S (value paths when ISV is nullptr)
     const uint2* ISV;      // (z id, z value) pairs parallel to IC_S, or nullptr (value paths load one pair)
     uint32_t T;            // z tiles
     uint32_t tile_width;   // z ids per tile (bitmap width)
@@ -373,8 +373,10 @@ __device__ __forceinline__ void cta_expand_flat(const RowCtx& c, uint32_t e0, ui
                 }
                 const uint32_t excl = lo ? cc->st.seg.incl[lo - 1] : 0u;
                 const uint32_t j = cc->st.seg.s0[lo] + (ci - excl);
-                z[u] = act ? ld_keep(&c.IC_S[j], pol) : kEmpty32;
-                if (Sink::kValues) v[u] = act ? ld_keep(&c.VS[j], pol) : 0u;
+                if (Sink::kValues && c.ISV != nullptr)
+                    load_cand<true, true>(c, j, act, pol, z[u], v[u]);
+                else
+                    load_cand<false, Sink::kValues>(c, j, act, pol, z[u], v[u]);
             }
             uint32_t b[kUnroll];
 #pragma unroll

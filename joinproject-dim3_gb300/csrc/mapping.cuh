@@ -194,8 +194,9 @@ static __global__ void k_scatter_r(const uint2* __restrict__ Pm, uint64_t n, uin
 
 // S CSR by (y id, z tile): z ids into ic and, beside them, z values into vs
 // (the write pass emits values without a gather through id2z).
-// isv (optional): the z id and z value of each entry side by side, for the
-// expansion paths that emit values (one 8-byte load or copy per candidate).
+// vs, isv (either may be null): the z values beside the ids, and the z id
+// and z value of each entry side by side for the expansion paths that emit
+// values (one 8-byte load or copy per candidate).
 static __global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t* __restrict__ zid, uint64_t n, uint32_t T,
                             uint32_t tile_shift, uint32_t* __restrict__ cursor, uint32_t* __restrict__ ic,
                             uint32_t* __restrict__ vs, uint2* __restrict__ isv) {
@@ -204,7 +205,7 @@ static __global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t*
         uint32_t zi = zid[i];
         uint32_t pos = atomic_inc_agg(cursor, (uint64_t)q.y * T + (zi >> tile_shift));
         ic[pos] = zi;
-        vs[pos] = q.x;
+        if (vs) vs[pos] = q.x;
         if (isv) isv[pos] = make_uint2(zi, q.x);
     }
 }
