@@ -208,6 +208,11 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
 // whose S row bounds over all z tiles fit the staging table: the bounds
 // (T + 1 per entry) are read once for the row, so each tile's chunks come
 // from shared memory -- no global round trip and two barriers per tile.
+#ifndef DIM3G_DYN_PIECE
+#define DIM3G_DYN_PIECE 512
+#endif
+constexpr uint32_t kDynPiece = DIM3G_DYN_PIECE;  // candidates a warp takes at a time (staged bitmap rows)
+
 template <class Sink>
 __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, uint32_t ne, uint32_t* bm,
                                                   Sink& sink, CtaChunks* cc) {
@@ -234,31 +239,41 @@ __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, 
             if (__any_sync(0xffffffffu, inc < len)) raise_error(c.err, kErrCountRange);  // 32-bit prefix wrapped
             if (lane == 31) cc->ctot[k] = inc;
         }
+        if (threadIdx.x == 0) cc->n = 0;  // the tile's piece counter
         __syncthreads();  // the tile's bitmap cleared, its chunk totals written
         const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
         const uint32_t inc = warp_incl_scan(v);
         if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
         const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-        const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
-        const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
         TileBitmap set{bm, lo};
-        for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
-            const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
-            const uint32_t cex = cin - ctot;
-            if (cex >= p1) break;
-            if (ctot == 0) continue;
-            const uint32_t i = k * 32 + lane;
-            Chunk ch;
-            ch.s0 = i < ne ? bnd[i * TB + t] : 0u;
-            ch.len = i < ne ? bnd[i * TB + t + 1] - ch.s0 : 0u;
-            ch.incl = warp_incl_scan(ch.len);
-            ch.excl = ch.incl - ch.len;
-            ch.total = ctot;
-            const uint32_t plo = p0 > cex ? p0 - cex : 0u, phi = p1 < cin ? p1 - cex : ctot;
-            expand_piece(c, ch, plo, phi, set, sink, pol);
+        // pieces of kDynPiece candidates taken from a shared counter: a warp
+        // slowed by short segments takes fewer, so the tile's barrier waits
+        // on at most one piece
+        for (;;) {
+            uint32_t p0 = 0;
+            if (lane == 0) p0 = atomicAdd(&cc->n, kDynPiece);
+            p0 = __shfl_sync(0xffffffffu, p0, 0);
+            if (p0 >= total) break;
+            const uint32_t p1 = min(p0 + kDynPiece, total);
+            for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); k < nch; k++) {
+                const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
+                const uint32_t cex = cin - ctot;
+                if (cex >= p1) break;
+                if (ctot == 0) continue;
+                const uint32_t i = k * 32 + lane;
+                Chunk ch;
+                ch.s0 = i < ne ? bnd[i * TB + t] : 0u;
+                ch.len = i < ne ? bnd[i * TB + t + 1] - ch.s0 : 0u;
+                ch.incl = warp_incl_scan(ch.len);
+                ch.excl = ch.incl - ch.len;
+                ch.total = ctot;
+                const uint32_t plo = p0 > cex ? p0 - cex : 0u, phi = p1 < cin ? p1 - cex : ctot;
+                expand_piece(c, ch, plo, phi, set, sink, pol);
+            }
         }
         __syncthreads();  // every insert into this tile done before the next clear
     }
+    if (threadIdx.x == 0) cc->n = 0;  // the round-robin walk's deferred-chunk count starts at 0
 }
 
 // Classes 3/4: the whole CTA expands row x one z tile at a time into a
