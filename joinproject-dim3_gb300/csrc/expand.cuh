@@ -420,10 +420,14 @@ __device__ __forceinline__ void balanced_stage(const RowCtx& c, uint32_t eb, uin
 // at the next barrier while another expands a long chunk alone.  No barrier.
 // s0 / len / ctot: the staged segment starts and lengths and the chunk
 // totals (a CtaChunks' arrays, or a prefetched row's).
+// dyn (optional, zeroed before the barrier that precedes this): a shared
+// counter from which the warps take pieces of dyn_piece candidates instead
+// of equal static shares.
 template <class Set, class Sink>
 __device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Set& set, Sink& sink,
                                                 const uint32_t* s0a, const uint32_t* lena, const uint32_t* ctota,
-                                                uint64_t pol, uint32_t wib, uint32_t nw) {
+                                                uint64_t pol, uint32_t wib, uint32_t nw, uint32_t* dyn = nullptr,
+                                                uint32_t dyn_piece = 0) {
     const uint32_t lane = lane_id();
     const uint32_t nch = (ne + 31) >> 5;
     // prefix of the chunk totals (every warp computes it; nch <= 32)
@@ -431,8 +435,19 @@ __device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Se
     const uint32_t inc = warp_incl_scan(v);
     if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-    const uint32_t piece = total / nw + (total % nw ? 1u : 0u);
-    const uint32_t p0 = min(wib * piece, total), p1 = min(p0 + piece, total);
+    const uint32_t piece = dyn ? dyn_piece : total / nw + (total % nw ? 1u : 0u);
+    for (uint32_t round = 0;; round++) {
+    uint32_t p0;
+    if (dyn) {
+        p0 = 0;
+        if (lane == 0) p0 = atomicAdd(dyn, piece);
+        p0 = __shfl_sync(0xffffffffu, p0, 0);
+        if (p0 >= total) break;
+    } else {
+        if (round) break;
+        p0 = min(wib * piece, total);
+    }
+    const uint32_t p1 = min(p0 + piece, total);
     // first chunk holding candidate p0: chunks with incl <= p0 form a prefix
     for (uint32_t k = __popc(__ballot_sync(0xffffffffu, lane < nch && inc <= p0)); p0 < p1 && k < nch; k++) {
         const uint32_t cin = __shfl_sync(0xffffffffu, inc, k), ctot = __shfl_sync(0xffffffffu, v, k);
@@ -447,6 +462,7 @@ __device__ __forceinline__ void balanced_expand(const RowCtx& c, uint32_t ne, Se
         ch.total = ctot;
         const uint32_t lo = p0 > cex ? p0 - cex : 0u, hi = p1 < cin ? p1 - cex : ctot;
         expand_piece(c, ch, lo, hi, set, sink, pol);
+    }
     }
 }
 

@@ -130,6 +130,13 @@ struct HashSink {
     }
 };
 
+#ifndef DIM3G_BLOCK_DYN_PIECE
+#define DIM3G_BLOCK_DYN_PIECE 0
+#endif
+// block-class rows: candidates a warp takes at a time from a shared counter
+// (0: equal static shares)
+constexpr uint32_t kBlockDynPiece = DIM3G_BLOCK_DYN_PIECE;
+
 // ---- row bodies (shared by the one-join kernels below and the many-query
 // kernels of batch.cuh)
 
@@ -184,13 +191,20 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
         const uint64_t pol = l2_keep_policy();
         const uint32_t nw = blockDim.x >> 5;
         balanced_stage(c, e0, ne, 0, c.T, cc, pol, wib, nw);
+        uint32_t* dyn = nullptr;
+        if (kBlockDynPiece) {
+            if (threadIdx.x == 0) cc->n = 0;
+            dyn = &cc->n;
+        }
         __syncthreads();
         if (bm) {
             TileBitmap set{smem, 0};
-            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw);
+            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw, dyn,
+                            kBlockDynPiece);
         } else {
             HashSet set{smem, lg, c.err};
-            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw);
+            balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw, dyn,
+                            kBlockDynPiece);
         }
         return;
     }
@@ -209,7 +223,7 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
 // (T + 1 per entry) are read once for the row, so each tile's chunks come
 // from shared memory -- no global round trip and two barriers per tile.
 #ifndef DIM3G_DYN_PIECE
-#define DIM3G_DYN_PIECE 512
+#define DIM3G_DYN_PIECE 256
 #endif
 constexpr uint32_t kDynPiece = DIM3G_DYN_PIECE;  // candidates a warp takes at a time (staged bitmap rows)
 
