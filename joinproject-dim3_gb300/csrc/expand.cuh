@@ -80,25 +80,9 @@ __device__ __forceinline__ uint32_t ceil_log2(uint32_t v) { return v <= 1 ? 0 : 
 
 // Insert z into an open-addressing set of 2^lg 32-bit slots in shared memory.
 // Returns true for the first insertion of z.
-#ifndef DIM3G_CAS_FIRST
-#define DIM3G_CAS_FIRST 0
-#endif
 __device__ __forceinline__ bool smem_set_insert(uint32_t* tab, uint32_t lg, uint32_t z, uint32_t* err) {
     const uint32_t mask = (1u << lg) - 1;
     uint32_t h = (z * 0x9E3779B1u) >> (32 - lg);
-    if (DIM3G_CAS_FIRST) {
-        // the compare-and-swap's old value answers every case of a probe
-        // (empty: claimed; z: already in; another key: next slot) in one
-        // shared-memory operation
-        for (uint32_t p = 0; p <= mask; p++) {
-            const uint32_t prev = atomicCAS(&tab[h], kEmpty32, z);
-            if (prev == kEmpty32) return true;
-            if (prev == z) return false;
-            h = (h + 1) & mask;
-        }
-        raise_error(err, kErrTableFull);
-        return false;
-    }
     volatile uint32_t* vt = tab;
     for (uint32_t p = 0; p <= mask; p++) {
         uint32_t cur = vt[h];
