@@ -52,11 +52,6 @@ namespace {
         launches++;                        \
     } while (0)
 
-uint64_t next_pow2(uint64_t v) {
-    uint64_t p = 1;
-    while (p < v) p <<= 1;
-    return p;
-}
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Offsets of typed arrays inside one device allocation.
@@ -132,6 +127,8 @@ struct dim3g_relset {
     uint32_t nrel = 0;
     std::vector<RelIn> h_in;
     std::vector<uint64_t> h_tup_off, h_tab_off;
+    std::vector<uint64_t> h_cap;  // sketch-sized table slots per relation (when sized)
+    bool sized = false;           // tables from h_cap (else from the tuple counts)
     uint64_t ntot = 0, tabtot = 0, yt_cap = 0;
     uint32_t tile_lg = 19;
     char* mem = nullptr;
@@ -164,7 +161,8 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
         if ((uintptr_t)rels[r].d_pairs & 7u) return I::fail(ctx, DIM3G_ERR_INVALID, "relation %u: pairs not 8-byte aligned", r);
         s->h_in[r] = RelIn{(const uint2*)rels[r].d_pairs, rels[r].n};
         s->h_tup_off[r + 1] = s->h_tup_off[r] + rels[r].n;
-        const uint64_t cap = next_pow2(rels[r].n * 2 < 1024 ? 1024 : rels[r].n * 2);
+        const uint64_t full = next_pow2(rels[r].n * 2 < 1024 ? 1024 : rels[r].n * 2);
+        const uint64_t cap = s->sized && s->h_cap[r] < full ? s->h_cap[r] : full;
         s->h_tab_off[r + 1] = s->h_tab_off[r] + cap;
         yt_guess += 2 * rels[r].n + 2;
     }
@@ -209,6 +207,7 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
     P.tup_off = (const uint64_t*)(m + o_tup);
     P.tab_off = (const uint64_t*)(m + o_tab);
     P.nrel = n;
+    P.probe_lim = s->sized ? (uint32_t)kSizedProbeLimit : 0u;
     P.ntot = s->ntot;
     P.TF = (unsigned long long*)(m + o_TF);
     P.TY = (unsigned long long*)(m + o_TY);
@@ -237,6 +236,82 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
     BCU(cudaMemcpy((void*)P.tup_off, s->h_tup_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy((void*)P.tab_off, s->h_tab_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
     return DIM3G_OK;
+}
+
+// Table sizes from a distinct-key sketch of every relation's two columns
+// (mapping.cuh): relation r's value -> id tables get s->h_cap[r] slots, about
+// table_slack_pct percent of its larger column's distinct keys, instead of
+// twice its tuple count.  The tables of a set whose relations repeat keys --
+// 1e3..1e6 distinct values over up to 4e6 tuples in a mixed batch -- then
+// shrink several times, and with them the build's memsets and id scans.  One
+// pass, synchronised, at creation; a build whose tables overflow the probe
+// bound (the data changed, or the estimate was low) is redone with
+// tuple-sized tables by the caller.
+int relset_sketch(dim3g_relset* s, const dim3g_relation* rels, uint32_t n) {
+    dim3g_ctx* ctx = s->ctx;
+    int64_t on = 1, slack = 150;
+    dim3g_get_param(ctx, "sized_tables", &on);
+    dim3g_get_param(ctx, "table_slack_pct", &slack);
+    s->sized = false;
+    s->h_cap.assign(n, 0);
+    if (!on || n == 0) return DIM3G_OK;
+    std::vector<RelIn> in(n);
+    std::vector<uint64_t> off(n + 1, 0);
+    for (uint32_t r = 0; r < n; r++) {
+        if (!rels[r].d_pairs && rels[r].n) return I::fail(ctx, DIM3G_ERR_INVALID, "relation %u: null pairs", r);
+        if ((uintptr_t)rels[r].d_pairs & 7u) return I::fail(ctx, DIM3G_ERR_INVALID, "relation %u: pairs not 8-byte aligned", r);
+        in[r] = RelIn{(const uint2*)rels[r].d_pairs, rels[r].n};
+        off[r + 1] = off[r] + rels[r].n;
+    }
+    if (off[n] == 0 || off[n] >= 0xFFFFFFFFull) return DIM3G_OK;  // nothing to size / refused by the plan
+    Layout L;
+    const size_t o_in = L.add<RelIn>(n), o_off = L.add<uint64_t>(n + 1), o_regs = L.add<uint32_t>((uint64_t)2 * n * kSketchRegs),
+                 o_sum = L.add<double2>(2 * (uint64_t)n);
+    char* m = nullptr;
+    if (cudaMalloc(&m, L.total) != cudaSuccess) {
+        cudaGetLastError();
+        return DIM3G_OK;  // no room for the sketch: tuple-sized tables
+    }
+    cudaStream_t st = I::stream(ctx);
+    RelPools P{};
+    P.in = (const RelIn*)(m + o_in);
+    P.tup_off = (const uint64_t*)(m + o_off);
+    P.nrel = n;
+    P.ntot = off[n];
+    uint32_t* regs = (uint32_t*)(m + o_regs);
+    double2* sums = (double2*)(m + o_sum);
+    std::vector<double2> h(2 * (size_t)n);
+    cudaError_t e = cudaMemcpyAsync((void*)P.in, in.data(), n * sizeof(RelIn), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((void*)P.tup_off, off.data(), (n + 1) * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(regs, 0, (size_t)2 * n * kSketchRegs * 4, st);
+    if (e == cudaSuccess) {
+        k_rel_sketch<<<elem_grid(P.ntot, I::sm_count(ctx)), 256, 0, st>>>(P, regs);
+        k_rel_sketch_sum<<<(2 * n + 7) / 8, 256, 0, st>>>(regs, 2 * n, sums);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), sums, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(m);
+    if (e != cudaSuccess) return I::fail(ctx, DIM3G_ERR_CUDA, "relation set sketch: %s", cudaGetErrorString(e));
+    I::add_launches(ctx, 2);
+    for (uint32_t r = 0; r < n; r++) {
+        const double ef = sketch_estimate(h[2 * r].x, (uint32_t)h[2 * r].y);
+        const double ey = sketch_estimate(h[2 * r + 1].x, (uint32_t)h[2 * r + 1].y);
+        const uint64_t full = next_pow2(rels[r].n * 2 < 1024 ? 1024 : rels[r].n * 2);
+        s->h_cap[r] = sketch_capacity(ef > ey ? ef : ey, full, (uint32_t)slack);
+        if (s->h_cap[r] < full) s->sized = true;
+    }
+    return DIM3G_OK;
+}
+
+// After a build: a sketch-sized table overflowed its probe bound.  Returns
+// true when the set was re-planned with tuple-sized tables (build again).
+bool relset_unsize(dim3g_relset* s, const dim3g_relation* rels, int* rc) {
+    *rc = DIM3G_OK;
+    if (!s->sized || !((uint32_t)s->h_need[1] & kErrProbeLimit)) return false;
+    s->sized = false;
+    *rc = relset_plan(s, rels, s->nrel, s->yt_cap);
+    return true;
 }
 
 // The build launches (stream ordered; capturable).
@@ -579,12 +654,16 @@ int query_results(dim3g_relset* s, const QueryScratch& qs, const QueryPlan& qp, 
 int relset_build_sync(dim3g_relset* s, const dim3g_relation* rels) {
     dim3g_ctx* ctx = s->ctx;
     cudaStream_t st = I::stream(ctx);
-    for (int attempt = 0; attempt < 2; attempt++) {
+    for (int attempt = 0; attempt < 3; attempt++) {
         uint64_t launches = 0;
         int r = relset_enqueue_build(s, st, launches);
         I::add_launches(ctx, launches);
         if (r) return r;
         BCU(cudaStreamSynchronize(st));
+        if (relset_unsize(s, rels, &r)) {
+            if (r) return r;
+            continue;
+        }
         const uint64_t need = s->h_need[0];
         const uint32_t err = (uint32_t)s->h_need[1];
         if (need <= s->yt_cap) {
@@ -662,6 +741,7 @@ int dim3g_relset_create(dim3g_ctx* ctx, const dim3g_relation* rels, uint32_t n, 
     int r = cudaMallocHost((void**)&s->h_need, 16) == cudaSuccess ? DIM3G_OK
                                                                    : I::fail(ctx, DIM3G_ERR_NOMEM, "pinned allocation failed");
     if (!r) r = set_batch_attributes(ctx);
+    if (!r) r = relset_sketch(s, rels, n);
     if (!r) r = relset_plan(s, rels, n, 0);
     if (!r) r = relset_build_sync(s, rels);
     if (r) {
@@ -721,6 +801,7 @@ int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_q
     if (!r && (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess))
         r = I::fail(ctx, DIM3G_ERR_CUDA, "event creation failed");
     if (!r) r = set_batch_attributes(ctx);
+    if (!r) r = relset_sketch(&b->set, b->rels.data(), 2 * n);
     if (!r) r = relset_plan(&b->set, b->rels.data(), 2 * n, 0);
     if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), n, b->qp);
     if (!r && b->qp.has_count) r = ensure_agg_scratch(&b->set, b->set.qs);
@@ -738,13 +819,21 @@ int dim3g_batch_run(dim3g_batch* b, dim3g_query* q) {
     dim3g_ctx* ctx = b->set.ctx;
     BCU(cudaSetDevice(I::device(ctx)));
     cudaStream_t st = I::stream(ctx);
-    for (int attempt = 0; attempt < 2; attempt++) {
+    for (int attempt = 0; attempt < 3; attempt++) {
         BCU(cudaEventRecord(b->ev0, st));
         BCU(cudaGraphLaunch(b->exec, st));
         BCU(cudaEventRecord(b->ev1, st));
         BCU(cudaStreamSynchronize(st));
         I::add_launches(ctx, b->launches_per_run);
         cudaEventElapsedTime(&b->ms_last, b->ev0, b->ev1);
+        int r = DIM3G_OK;
+        if (relset_unsize(&b->set, b->rels.data(), &r)) {
+            // a sketch-sized table overflowed: tuple-sized tables from now on
+            if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), b->qp.nq, b->qp);
+            if (!r) r = batch_capture(b);
+            if (r) return r;
+            continue;
+        }
         const uint64_t need = b->set.h_need[0];
         if (need <= b->set.yt_cap) {
             const uint32_t err = (uint32_t)b->set.h_need[1];
@@ -756,7 +845,7 @@ int dim3g_batch_run(dim3g_batch* b, dim3g_query* q) {
             return query_results(&b->set, b->set.qs, b->qp, q);
         }
         // the (y, f tile) key space outgrew its pool: re-plan and capture
-        int r = relset_plan(&b->set, b->rels.data(), (uint32_t)b->rels.size(), need);
+        r = relset_plan(&b->set, b->rels.data(), (uint32_t)b->rels.size(), need);
         if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), b->qp.nq, b->qp);
         if (!r) r = batch_capture(b);
         if (r) return r;

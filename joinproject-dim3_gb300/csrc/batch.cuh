@@ -57,13 +57,17 @@ struct SegCursor {
     }
 };
 
-// CTA-contiguous element ranges: CTA b covers [b*per, (b+1)*per) in rounds
-// of blockDim, so a thread's segment changes rarely.
-#define DIM3G_FOR_CHUNK(i, n)                                                           \
-    const uint64_t per_ = ((n) + gridDim.x - 1) / gridDim.x;                            \
-    const uint64_t c0_ = (uint64_t)blockIdx.x * per_;                                   \
-    const uint64_t c1_ = c0_ + per_ < (n) ? c0_ + per_ : (n);                           \
-    for (uint64_t i = c0_ + threadIdx.x; i < c1_; i += blockDim.x)
+// Grid-ordered element ranges: in round k CTA b takes the elements
+// [(k * G + b) * blockDim, + blockDim), G the grid, so the whole grid works
+// inside a window of about G * blockDim consecutive elements that moves
+// through the relations in order.  The random-address updates of the index
+// build (table slots, degree and cursor atomics, the CSR scatter) then fall
+// in the few relations under the window, whose tables and CSR slices stay in
+// L2, instead of in all of the set at once (CTA-contiguous ranges put the
+// grid's CTAs in as many different relations).  The segment of an element is
+// looked up again when a thread's next element lies in another relation.
+#define DIM3G_FOR_CHUNK(i, n) \
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (uint64_t)gridDim.x * blockDim.x)
 
 // Adds pred over the calling lanes to ctr[s], one atomic per group of lanes
 // sharing s.
@@ -89,7 +93,8 @@ struct RelDev {
     uint64_t nf, ny;    // distinct f, distinct y
     uint64_t fbase, ybase;  // first global f id / y id
     uint64_t yt_base;   // first key of the (y, f tile) key space
-    uint32_t T, tile_shift, tile_width, pad;
+    uint32_t T, tile_shift, tile_width;
+    uint32_t probe_lim; // longest probe of the tables (0: the whole table)
 };
 
 // Pools of one relation set (device pointers).
@@ -99,6 +104,7 @@ struct RelPools {
     const uint64_t* tup_off;  // nrel + 1
     const uint64_t* tab_off;  // nrel + 1
     uint32_t nrel;
+    uint32_t probe_lim;       // sketch-sized tables: longest probe (0: tuple-sized tables)
     uint64_t ntot;            // sum of tuples
     unsigned long long* TF;
     unsigned long long* TY;
@@ -124,7 +130,7 @@ struct RelPools {
 };
 
 __device__ __forceinline__ DevTable rel_table(unsigned long long* pool, const RelDev& r) {
-    return DevTable{pool + r.tab_off, r.tab_cap - 1};
+    return DevTable{pool + r.tab_off, r.tab_cap - 1, r.probe_lim};
 }
 
 static __global__ void k_ix_insert(RelPools P) {
@@ -133,11 +139,45 @@ static __global__ void k_ix_insert(RelPools P) {
         const uint32_t r = sc.at(i);
         const uint2 t = P.in[r].pairs[i - sc.lo];
         const uint64_t to = __ldg(&P.tab_off[r]), cap = __ldg(&P.tab_off[r + 1]) - to;
-        const bool nf = table_insert(DevTable{P.TF + to, cap - 1}, t.x, P.err);
-        const bool ny = table_insert(DevTable{P.TY + to, cap - 1}, t.y, P.err);
+        const bool nf = table_insert(DevTable{P.TF + to, cap - 1, P.probe_lim}, t.x, P.err);
+        const bool ny = table_insert(DevTable{P.TY + to, cap - 1, P.probe_lim}, t.y, P.err);
         warp_count_by_seg(P.nf_cnt, r, nf);
         warp_count_by_seg(P.ny_cnt, r, ny);
     }
+}
+
+// Distinct-key sketches of every relation's two columns (kSketchRegs
+// registers per column, zeroed by the caller): relation r's first column at
+// regs + 2 r kSketchRegs, its y column after it.  Grid-ordered, so a warp's
+// updates fall in one or two relations' registers.
+static __global__ void k_rel_sketch(RelPools P, uint32_t* regs) {
+    SegCursor sc{P.tup_off, P.nrel};
+    DIM3G_FOR_CHUNK(i, P.ntot) {
+        const uint32_t r = sc.at(i);
+        const uint2 t = P.in[r].pairs[i - sc.lo];
+        uint32_t* rr = regs + (uint64_t)2 * r * kSketchRegs;
+        sketch_add_if_larger(rr, t.x);
+        sketch_add_if_larger(rr + kSketchRegs, t.y);
+    }
+}
+
+// One warp per column: (sum of 2^-register, zero registers).
+static __global__ void k_rel_sketch_sum(const uint32_t* __restrict__ regs, uint32_t ncol, double2* out) {
+    const uint32_t col = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (col >= ncol) return;
+    const uint32_t* r = regs + (uint64_t)col * kSketchRegs;
+    double sum = 0;
+    uint32_t zeros = 0;
+    for (uint32_t k = lane; k < kSketchRegs; k += 32) {
+        const uint32_t v = r[k];
+        sum += ldexp(1.0, -(int)v);
+        zeros += v == 0;
+    }
+    for (int o = 16; o; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        zeros += __shfl_xor_sync(0xffffffffu, zeros, o);
+    }
+    if (lane == 0) out[col] = make_double2(sum, (double)zeros);
 }
 
 // One CTA: per-relation id bases, z tiling and (y, tile) key ranges.
@@ -171,7 +211,7 @@ static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t 
             d.T = (uint32_t)T;
             d.tile_shift = T > 1 ? tile_lg : 31;
             d.tile_width = T > 1 ? (1u << tile_lg) : (uint32_t)(nf > 0 ? nf : 1);
-            d.pad = 0;
+            d.probe_lim = P.probe_lim;
             P.rel[r] = d;
             P.yoff[r] = d.ybase;
         }
@@ -183,6 +223,10 @@ static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t 
         P.yoff[P.nrel] = cy;
         *P.yt_need = ck + 1;
         if (ck + 1 > P.yt_cap) raise_error(P.err, kErrTableFull);
+        // a sketch-sized table overflowed its probe bound: some ids are
+        // missing, so no later kernel may use the tables (the host rebuilds
+        // with tuple-sized tables)
+        if (*(volatile uint32_t*)P.err & kErrProbeLimit) *P.yt_need = ~0ull;
     }
 }
 
@@ -310,8 +354,7 @@ static __global__ void k_q_ymap(QueryPools Q) {
         const RelDev& q = Q.rel[qn.q];
         const uint64_t y = i - sc.lo;
         if (y >= p.ny) continue;
-        const uint32_t g = table_find(DevTable{(unsigned long long*)Q.TY + q.tab_off, q.tab_cap - 1},
-                                      Q.id2y[p.ybase + y]);
+        const uint32_t g = table_find(rel_table((unsigned long long*)Q.TY, q), Q.id2y[p.ybase + y]);
         Q.ymap[i] = g == kNotFound ? (uint32_t)q.ny : g - (uint32_t)q.ybase;
     }
 }

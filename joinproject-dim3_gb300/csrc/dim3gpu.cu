@@ -189,11 +189,6 @@ int run_scan(dim3g_ctx* c, Src src, Dst dst, uint64_t n, uint64_t* bsum, unsigne
         if (r_) return r_;                       \
     } while (0)
 
-uint64_t next_pow2(uint64_t v) {
-    uint64_t p = 1;
-    while (p < v) p <<= 1;
-    return p;
-}
 
 unsigned grid_for(uint64_t n, int sm, int per_sm = 8, int block = 256) {
     uint64_t b = (n + block - 1) / block;
@@ -612,11 +607,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
                 sum += ldexp(1.0, -(int)r[k]);
                 zeros += r[k] == 0;
             }
-            const double M = kSketchRegs;
-            double e = 0.7213 / (1.0 + 1.079 / M) * M * M / sum;
-            if (e <= 2.5 * M && zeros) e = M * log(M / zeros);  // small-range estimate
-            const uint64_t cap = next_pow2((uint64_t)(c->prm.table_slack_pct / 100.0 * e) + 1024);
-            return cap < full ? cap : full;
+            return sketch_capacity(sketch_estimate(sum, zeros), full, c->prm.table_slack_pct);
         };
         capX = sized(hr.data(), fullP);
         capY = sized(hr.data() + kSketchRegs, fullP);

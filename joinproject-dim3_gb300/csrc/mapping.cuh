@@ -64,12 +64,43 @@ __device__ __forceinline__ uint32_t table_find(DevTable t, uint32_t key) {
 constexpr uint32_t kSketchLg = 11, kSketchRegs = 1u << kSketchLg;
 constexpr uint64_t kSizedProbeLimit = 1u << 12;
 
-__device__ __forceinline__ void sketch_add(uint32_t* r, uint32_t key) {
+// A key's register (the hash's top kSketchLg bits) and rank (leading zeros
+// of the rest, plus one).
+__device__ __forceinline__ uint2 sketch_slot(uint32_t key) {
     const unsigned long long h = mix64((unsigned long long)key + 0x9E3779B97F4A7C15ull);
-    const uint32_t idx = (uint32_t)(h >> (64 - kSketchLg));
     const unsigned long long w = h << kSketchLg;
-    const uint32_t rank = (w ? (uint32_t)__clzll(w) : 64u - kSketchLg) + 1;
-    atomicMax(&r[idx], rank);
+    return make_uint2((uint32_t)(h >> (64 - kSketchLg)), (w ? (uint32_t)__clzll(w) : 64u - kSketchLg) + 1);
+}
+__device__ __forceinline__ void sketch_add(uint32_t* r, uint32_t key) {
+    const uint2 s = sketch_slot(key);
+    atomicMax(&r[s.x], s.y);
+}
+
+inline uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// sketch_add without the atomic when the register already holds the rank
+// (most updates once the registers have filled).
+__device__ __forceinline__ void sketch_add_if_larger(uint32_t* r, uint32_t key) {
+    const uint2 s = sketch_slot(key);
+    if (__ldcg(&r[s.x]) < s.y) atomicMax(&r[s.x], s.y);
+}
+
+// HyperLogLog estimate (with the small-range correction) from a column's
+// register sum (sum of 2^-r) and count of zero registers; the table slots for
+// it, slack_pct slots per estimated key, a power of two no larger than full.
+inline double sketch_estimate(double sum, uint32_t zeros) {
+    const double M = kSketchRegs;
+    double e = 0.7213 / (1.0 + 1.079 / M) * M * M / sum;
+    if (e <= 2.5 * M && zeros) e = M * log(M / zeros);
+    return e;
+}
+inline uint64_t sketch_capacity(double est, uint64_t full, uint32_t slack_pct) {
+    const uint64_t cap = next_pow2((uint64_t)(slack_pct / 100.0 * est) + 1024);
+    return cap < full ? cap : full;
 }
 
 // Registers of P's first and y columns and Q's first column, kSketchRegs

@@ -90,6 +90,52 @@ def test_relset_golden_project_and_count(built, golden, params):
     c.close()
 
 
+@pytest.mark.parametrize("sized,slack", [(1, 150), (0, 150), (1, 5)])
+def test_relset_tables_sized_by_sketch(built, golden, sized, slack):
+    """The relation set's value -> id tables sized per relation by a
+    distinct-key sketch (smaller than tuple-sized ones: fewer device bytes),
+    tuple-sized, and sized far too small on purpose (5 % of the distinct
+    keys): the overfilled build is detected and redone with tuple-sized
+    tables.  Every query exact in each case."""
+    import dim3gpu
+    _, rels = _inputs(golden, CASES)
+    sizes = {}
+    for sz, sl in [(0, 150), (sized, slack)]:
+        c = dim3gpu.Context(0)
+        c.set_param("sized_tables", sz)
+        c.set_param("table_slack_pct", sl)
+        rs = dim3gpu.RelSet(c, rels)
+        sizes[(sz, sl)] = rs.bytes()
+        specs = _specs(golden, CASES, [dim3gpu.OP_PROJECT, dim3gpu.OP_COUNT])
+        _check(golden, specs, rs.join(specs))
+        rs.close()
+        c.close()
+    if sized and slack == 150:
+        assert sizes[(1, 150)] < sizes[(0, 150)], sizes
+    if sized and slack == 5:
+        assert sizes[(1, 5)] >= sizes[(0, 150)], sizes  # rebuilt with tuple-sized tables
+
+
+def test_batch_sized_tables_overflow_rebuilds(built, golden):
+    """A batch whose sketch-sized tables are too small (5 % slack): its first
+    run detects the overflow, re-plans with tuple-sized tables, re-captures
+    the graph and returns exact results; later runs replay the new graph."""
+    import dim3gpu
+    c = dim3gpu.Context(0)
+    c.set_param("table_slack_pct", 5)
+    names = ["grd_small", "zipf_1m_s001", "chung_lu_s005", "heavy_duplicates", "grd_sparse"]
+    _, rels = _inputs(golden, names)
+    pairs = [(rels[2 * i], rels[2 * i + 1]) for i in range(len(names))]
+    specs = _specs(golden, names, [dim3gpu.OP_PROJECT])
+    b = dim3gpu.Batch(c, pairs, specs)
+    small = b.info()["device_bytes"]
+    for _ in range(2):
+        _check(golden, specs, b.run())
+    assert b.info()["device_bytes"] > small
+    b.close()
+    c.close()
+
+
 def test_relset_cross_joins_match_oracle(ctx, golden):
     """Joins across cases (R of one, S of another, both orientations) against
     the oracle on the same relations."""
