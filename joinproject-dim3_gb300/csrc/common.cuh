@@ -94,6 +94,20 @@ __device__ __forceinline__ uint2 ld_keep2(const uint2* a, uint64_t pol) {
     return v;
 }
 __device__ __forceinline__ void st_stream(uint2* a, uint2 v) { __stcs(a, v); }
+// Asks L2 to fetch the bytes [lo, hi) (a hint: no data returns to the SM).
+// The range is shrunk to 16-byte boundaries inside it -- the bulk prefetch
+// wants a 16-byte aligned start and a multiple of 16 bytes -- and to at most
+// kPrefetchMax bytes, so nothing outside [lo, hi) is named.
+constexpr uint32_t kPrefetchMax = 32u << 10;
+__device__ __forceinline__ void l2_prefetch(const void* lo, const void* hi, uint64_t pol) {
+    const uint64_t a = (reinterpret_cast<uint64_t>(lo) + 15) & ~15ull;
+    uint64_t e = reinterpret_cast<uint64_t>(hi) & ~15ull;
+    if (e > a + kPrefetchMax) e = a + kPrefetchMax;
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(a), "r"((uint32_t)(e - a)),
+                     "l"(pol)
+                     : "memory");
+}
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ uint32_t lanemask_lt() {

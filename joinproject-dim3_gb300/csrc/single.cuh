@@ -227,6 +227,13 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
 #endif
 constexpr uint32_t kDynPiece = DIM3G_DYN_PIECE;  // candidates a warp takes at a time (staged bitmap rows)
 
+// With kTilePrefetch each S segment is prefetched into L2 by one bulk
+// prefetch a tile ahead (the first tile's while the row is staged).
+#ifndef DIM3G_TILE_PREFETCH
+#define DIM3G_TILE_PREFETCH 1
+#endif
+constexpr bool kTilePrefetch = DIM3G_TILE_PREFETCH != 0;
+
 template <class Sink>
 __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, uint32_t ne, uint32_t* bm,
                                                   Sink& sink, CtaChunks* cc) {
@@ -238,6 +245,7 @@ __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, 
         const uint32_t y = ld_keep(&c.IC_R[e0 + i], pol);
         const uint64_t r = (uint64_t)y * T;
         for (uint32_t k = 0; k <= T; k++) bnd[i * TB + k] = ld_keep(&c.JR_S[r + k], pol);
+        if (kTilePrefetch && c.ISV) l2_prefetch(c.ISV + bnd[i * TB], c.ISV + bnd[i * TB + 1], pol);
     }
     for (uint32_t t = 0; t < T; t++) {
         const uint32_t lo = t * c.tile_width;
@@ -246,6 +254,12 @@ __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, 
         uint4* b4 = reinterpret_cast<uint4*>(bm);
         for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
         if (t == 0) __syncthreads();  // the staged bounds
+        if (kTilePrefetch && t + 1 < T && c.ISV) {
+            // the next tile's segments into L2 while this tile expands (its
+            // candidate loads then hit L2 instead of waiting on DRAM)
+            for (uint32_t i = threadIdx.x; i < ne; i += blockDim.x)
+                l2_prefetch(c.ISV + bnd[i * TB + t + 1], c.ISV + bnd[i * TB + t + 2], pol);
+        }
         for (uint32_t k = wib; k < nch; k += nw) {
             const uint32_t i = k * 32 + lane;
             const uint32_t len = i < ne ? bnd[i * TB + t + 1] - bnd[i * TB + t] : 0u;
