@@ -104,6 +104,10 @@ int dim3g_get_stats(const dim3g_ctx* ctx, dim3g_stats* out);
  * memory by bulk copies -- exact, measured slower on the 2-hop),
  * "prefetch_rows" (1: block-class rows of the single pass fetched ahead by a
  * producer warp -- exact, measured slower on the 2-hop),
+ * "block_split" (1, default: the single pass runs block-class rows in three
+ * launches by hash-set size -- 2^(b-2), 2^(b-1) and 2^b slots for
+ * block_slots_log2 = b -- the two smaller with 256-thread CTAs, so more rows
+ * are in flight per SM; 0: one launch of 2^b-slot CTAs),
  * "keep_roles" (0: the larger relation drives the join, the reference's
  * swap at dim3.hpp:993-994, so a smaller R yields (S.first, R.first) pairs;
  * 1: R always drives and pairs are always (R.first, S.first) -- for joining

@@ -100,6 +100,7 @@ struct Params {
     uint32_t table_slack_pct = 150;  // sketch-sized table slots per estimated distinct key, percent
     uint32_t stream_rows = 0;  // single pass: bitmap-class rows streamed by TMA (stream.cuh)
     uint32_t prefetch_rows = 0;  // single pass, balanced walk: block-class rows fetched ahead (prefetch.cuh)
+    uint32_t block_split = 1;    // single pass: block-class rows in three launches by hash-set size
 };
 
 constexpr size_t kMaxSmemOptin = 227 * 1024;  // dynamic shared memory a CTA may opt into
@@ -113,7 +114,8 @@ struct Scalars {
     unsigned long long cursor_at[3]; // single-pass cursor after the bitmap / block / warp kernel
     unsigned long long dense_base;   // single-pass start of the dense block's pairs (~0: past the capacity)
     unsigned int err;
-    unsigned int next_row[4];      // dynamic row counters of the CTA classes
+    unsigned long long nrows_b[3];  // block-class rows by hash-set size (single pass, block_split)
+    unsigned int next_row[8];      // dynamic row counters of the CTA classes (4..6: block_split launches)
     unsigned int pad;
 };
 
@@ -742,6 +744,18 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* list_t = lists + 3 * (uint64_t)n;
     SCAN(ClassSrc{cls, 1}, ListDst{list_w, nullptr}, n, bsum2, &sc->nrows[1]);
     SCAN(ClassSrc{cls, 2}, ListDst{list_b, nullptr}, n, bsum2, &sc->nrows[2]);
+    const bool block_split = jp.single_pass && !jp.aggregate && !jp.count_only && !jp.sum.tiles &&
+                             c->prm.block_split && !(c->prm.prefetch_rows && c->prm.cta_rr == 3);
+    if (block_split) {
+        // the same rows again, ordered by hash-set size: u <= 2^(b-3), then
+        // u <= 2^(b-2), then the rest (b = block_lg; 2^lg slots for 2u keys)
+        const uint32_t b = c->prm.block_lg;
+        SCAN(BlockSizeSrc{cls, ucap, 0u, 1u << (b - 3)}, ListDst{list_b, nullptr}, n, bsum2, &sc->nrows_b[0]);
+        SCAN(BlockSizeSrc{cls, ucap, 1u << (b - 3), 1u << (b - 2)}, ListDst{list_b, &sc->nrows_b[0]}, n, bsum2,
+             &sc->nrows_b[1]);
+        SCAN(BlockSizeSrc{cls, ucap, 1u << (b - 2), 0xFFFFFFFFu}, ListDst{list_b, &sc->nrows_b[0], &sc->nrows_b[1]}, n,
+             bsum2, &sc->nrows_b[2]);
+    }
     // bitmap rows: class 4 (huge) first, then class 3
     SCAN(ClassSrc{cls, 4}, ListDst{list_m, nullptr}, n, bsum2, &sc->nrows[4]);
     SCAN(ClassSrc{cls, 3}, ListDst{list_m, &sc->nrows[4]}, n, bsum2, &sc->nrows[3]);
@@ -844,9 +858,22 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
             const size_t ss_p = (((size_t)1 << c->prm.block_lg) + (size_t)kPfWorkers * kStage) * 4;
             k_single_block_pf<<<resident_grid(k_single_block_pf, kPfThreads, ss_p, sm), kPfThreads, ss_p, st>>>(
                 rc, rs, L.b, L.nb, c->prm.block_lg);
+        } else if (block_split) {
+            // three launches over list_b's three parts, smallest sets first
+            const uint32_t b = c->prm.block_lg;
+            const unsigned long long* skip[3][2] = {{nullptr, nullptr}, {&sc->nrows_b[0], nullptr},
+                                                    {&sc->nrows_b[0], &sc->nrows_b[1]}};
+            for (uint32_t k = 0; k < 3; k++) {
+                const int thr = k < 2 ? (int)kBlockSplitThreads : blk_b;
+                const uint32_t lg = b - 2 + k;
+                const size_t ss = ((size_t)1 << lg << 2) + (size_t)(thr / 32) * kStage * 4;
+                k_single_block<<<resident_grid(k_single_block, thr, ss, sm), thr, ss, st>>>(
+                    rc, rs, L.b, &sc->nrows_b[k], lg, skip[k][0], skip[k][1], 4 + k);
+                CHECK_LAUNCH();
+            }
         } else {
-            k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(rc, rs, L.b, L.nb,
-                                                                                              c->prm.block_lg);
+            k_single_block<<<resident_grid(k_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(
+                rc, rs, L.b, L.nb, c->prm.block_lg, nullptr, nullptr, 2);
         }
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[6], st));
@@ -1304,6 +1331,9 @@ int dim3g_set_param(dim3g_ctx* c, const char* name, int64_t v) {
     } else if (!strcmp(name, "table_slack_pct")) {
         if (v < 5 || v > 1000) return fail(c, DIM3G_ERR_INVALID, "table_slack_pct must be in 5..1000");
         c->prm.table_slack_pct = (uint32_t)v;
+    } else if (!strcmp(name, "block_split")) {
+        if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "block_split must be 0 or 1");
+        c->prm.block_split = (uint32_t)v;
     } else if (!strcmp(name, "prefetch_rows")) {
         if (v != 0 && v != 1) return fail(c, DIM3G_ERR_INVALID, "prefetch_rows must be 0 or 1");
         c->prm.prefetch_rows = (uint32_t)v;
@@ -1334,6 +1364,7 @@ int dim3g_get_param(const dim3g_ctx* c, const char* name, int64_t* v) {
     else if (!strcmp(name, "keep_roles")) *v = c->prm.keep_roles ? 1 : 0;
     else if (!strcmp(name, "stream_rows")) *v = c->prm.stream_rows;
     else if (!strcmp(name, "prefetch_rows")) *v = c->prm.prefetch_rows;
+    else if (!strcmp(name, "block_split")) *v = c->prm.block_split;
     else if (!strcmp(name, "sized_tables")) *v = c->prm.sized_tables ? 1 : 0;
     else if (!strcmp(name, "table_slack_pct")) *v = c->prm.table_slack_pct;
     else return DIM3G_ERR_INVALID;

@@ -787,12 +787,23 @@ struct ClassSrc {
     uint8_t want;
     __device__ uint64_t operator()(uint64_t i) const { return cls[i] == want ? 1u : 0u; }
 };
-// list[*base + rank] = row (base: count of rows placed before this class).
+// Block-class (class 2) rows whose distinct bound u is in (lo, hi].
+struct BlockSizeSrc {
+    const uint8_t* cls;
+    const uint32_t* ucap;
+    uint32_t lo, hi;
+    __device__ uint64_t operator()(uint64_t i) const {
+        return cls[i] == 2 && ucap[i] > lo && ucap[i] <= hi ? 1u : 0u;
+    }
+};
+// list[*base + *base2 + rank] = row (bases: counts of rows placed before
+// this class; either may be null).
 struct ListDst {
     uint32_t* list;
     const unsigned long long* base;
+    const unsigned long long* base2 = nullptr;
     __device__ void operator()(uint64_t i, uint64_t e, uint64_t v) const {
-        if (v) list[(base ? *base : 0) + e] = (uint32_t)i;
+        if (v) list[(base ? *base : 0) + (base2 ? *base2 : 0) + e] = (uint32_t)i;
     }
 };
 struct OffDst {

@@ -136,6 +136,11 @@ struct HashSink {
 // block-class rows: candidates a warp takes at a time from a shared counter
 // (0: equal static shares)
 constexpr uint32_t kBlockDynPiece = DIM3G_BLOCK_DYN_PIECE;
+// CTA width of the two smaller-set block launches (block_split)
+#ifndef DIM3G_BLOCK_SPLIT_THREADS
+#define DIM3G_BLOCK_SPLIT_THREADS 256
+#endif
+constexpr uint32_t kBlockSplitThreads = DIM3G_BLOCK_SPLIT_THREADS;
 
 // ---- row bodies (shared by the one-join kernels below and the many-query
 // kernels of batch.cuh)
@@ -166,17 +171,67 @@ __device__ __forceinline__ void single_warp_row(const RowCtx& c, uint32_t x, uin
     __syncwarp();
 }
 
+// Row look-ahead for the bitmap class.  A CTA row starts with a chain of
+// dependent global round trips -- the row counter's atomic, the row id, the
+// row's header (x value, distinct bound, R bounds) -- before its own staging
+// loads, with the whole CTA waiting.  With RowAhead, thread 0 walks that
+// chain for the NEXT row once this row's first tile has started (the other
+// warps take its share through the tile's dynamic pieces) and leaves the
+// header in shared memory, read by every thread after the row's closing
+// barrier.  (Block-class rows are too short for it: their static shares
+// would wait on thread 0, and dynamic pieces cost them more than the chain.)
+struct RowHead {
+    uint32_t ri, xv, u, e0, e1;  // ri >= the row count: no row
+};
+struct NoAhead {
+    __device__ __forceinline__ void run() {}
+};
+// Where the look-ahead reads from, set once per CTA (shared memory, so the
+// row loop holds no registers for it).
+struct AheadSrc {
+    const uint32_t* rows;
+    uint32_t* counter;
+    const uint32_t* id2x;
+    const uint32_t* ucap;
+    const uint32_t* JR_R;
+    uint32_t nrows;
+};
+static __shared__ AheadSrc s_ahead_src;
+struct RowAhead {
+    RowHead* dst;
+    __device__ __forceinline__ void run() {
+        if (threadIdx.x != 0) return;
+        const AheadSrc& a = s_ahead_src;
+        RowHead h{atomicAdd(a.counter, 1u), 0u, 0u, 0u, 0u};
+        if (h.ri < a.nrows) {
+            const uint32_t x = a.rows[h.ri];
+            h.xv = a.id2x[x];
+            h.u = a.ucap[x];
+            h.e0 = a.JR_R[x];
+            h.e1 = a.JR_R[x + 1];
+        }
+        *dst = h;
+    }
+};
+// Thread 0: the look-ahead's source and the first row's header (s_head[0]);
+// followed by a barrier in the caller.
+__device__ __forceinline__ void ahead_start(const RowCtx& c, const uint32_t* rows, uint32_t* counter, uint32_t nrows,
+                                            RowHead* s_head) {
+    if (threadIdx.x != 0) return;
+    s_ahead_src = AheadSrc{rows, counter, c.id2x, c.ucap, c.JR_R, nrows};
+    RowAhead{s_head}.run();
+}
+
 // Class 2: the whole CTA expands row x; a 2^block_lg-word table (hash set or
 // whole-domain bitmap) at smem, into each warp's sink (the caller sets its
 // x value and flushes it).  Called by all threads after a barrier that
 // follows the previous row; the caller's next call comes after another
 // barrier (the last warps may still be expanding when this returns).
-template <class Sink>
-__device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, uint32_t* smem, Sink& sink,
-                                                 uint32_t block_lg, CtaChunks* cc) {
+template <class Sink, class Ahead>
+__device__ __forceinline__ void block_row(const RowCtx& c, uint32_t u, uint32_t e0, uint32_t e1, uint32_t* smem,
+                                          Sink& sink, uint32_t block_lg, CtaChunks* cc, Ahead& ah) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    const uint32_t u = c.ucap[x];
     const bool bm = use_row_bitmap(c.m, u, block_lg);
     uint32_t lg = ceil_log2(2 * u);
     lg = lg < 5 ? 5 : (lg > block_lg ? block_lg : lg);
@@ -184,7 +239,7 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
     const uint32_t n4 = (bm ? row_bitmap_words(c.m) : (1u << lg)) / 4;
     uint4* t4 = reinterpret_cast<uint4*>(smem);
     for (uint32_t s = threadIdx.x; s < n4; s += blockDim.x) t4[s] = make_uint4(fill, fill, fill, fill);
-    const uint32_t e0 = c.JR_R[x], ne = c.JR_R[x + 1] - e0;
+    const uint32_t ne = e1 - e0;
     if (c.cta_rr == 3 && ne <= kRowBlk) {
         // balanced walk of one staging block: the table's clearing and the
         // staging share one barrier; the caller's next-row barrier ends it
@@ -197,6 +252,7 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
             dyn = &cc->n;
         }
         __syncthreads();
+        ah.run();
         if (bm) {
             TileBitmap set{smem, 0};
             balanced_expand(c, ne, set, sink, cc->st.seg.s0, cc->st.seg.incl, cc->ctot, pol, wib, nw, dyn,
@@ -209,13 +265,21 @@ __device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, ui
         return;
     }
     __syncthreads();
+    ah.run();
     if (bm) {
         TileBitmap set{smem, 0};
-        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink, cc);
+        cta_expand(c, e0, e1, wib, nw_lg, 0, c.T, set, sink, cc);
     } else {
         HashSet set{smem, lg, c.err};
-        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, 0, c.T, set, sink, cc);
+        cta_expand(c, e0, e1, wib, nw_lg, 0, c.T, set, sink, cc);
     }
+}
+
+template <class Sink>
+__device__ __forceinline__ void single_block_row(const RowCtx& c, uint32_t x, uint32_t* smem, Sink& sink,
+                                                 uint32_t block_lg, CtaChunks* cc) {
+    NoAhead na;
+    block_row(c, c.ucap[x], c.JR_R[x], c.JR_R[x + 1], smem, sink, block_lg, cc, na);
 }
 
 // Classes 3/4 with the balanced walk for a row of at most kRowBlk entries
@@ -234,9 +298,9 @@ constexpr uint32_t kDynPiece = DIM3G_DYN_PIECE;  // candidates a warp takes at a
 #endif
 constexpr bool kTilePrefetch = DIM3G_TILE_PREFETCH != 0;
 
-template <class Sink>
+template <class Sink, class Ahead>
 __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, uint32_t ne, uint32_t* bm,
-                                                  Sink& sink, CtaChunks* cc) {
+                                                  Sink& sink, CtaChunks* cc, Ahead& ah) {
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t T = c.T, TB = T + 1, nch = (ne + 31) >> 5;
     const uint64_t pol = l2_keep_policy();
@@ -269,6 +333,7 @@ __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, 
         }
         if (threadIdx.x == 0) cc->n = 0;  // the tile's piece counter
         __syncthreads();  // the tile's bitmap cleared, its chunk totals written
+        if (t == 0) ah.run();
         const uint32_t v = lane < nch ? cc->ctot[lane] : 0u;
         const uint32_t inc = warp_incl_scan(v);
         if (__any_sync(0xffffffffu, inc < v)) raise_error(c.err, kErrCountRange);
@@ -301,23 +366,22 @@ __device__ __forceinline__ void bitmap_row_staged(const RowCtx& c, uint32_t e0, 
         }
         __syncthreads();  // every insert into this tile done before the next clear
     }
+    if (T == 0) ah.run();
     if (threadIdx.x == 0) cc->n = 0;  // the round-robin walk's deferred-chunk count starts at 0
 }
 
 // Classes 3/4: the whole CTA expands row x one z tile at a time into a
 // bitmap at bm (words rounded up to uint4, at least 32), into each warp's
 // sink (the caller sets its x value and flushes it once for the row).
-template <class Sink>
-__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, uint32_t* bm, Sink& sink,
-                                                  CtaChunks* cc) {
+template <class Sink, class Ahead>
+__device__ __forceinline__ void bitmap_row(const RowCtx& c, uint32_t e0, uint32_t e1, uint32_t* bm, Sink& sink,
+                                           CtaChunks* cc, Ahead& ah) {
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t nw_lg = 31 - __clz(blockDim.x >> 5);
-    {
-        const uint32_t e0 = c.JR_R[x], ne = c.JR_R[x + 1] - e0;
-        if (c.cta_rr == 3 && ne <= kRowBlk && (uint64_t)ne * (c.T + 1) <= 2 * kRowBlk) {
-            bitmap_row_staged(c, e0, ne, bm, sink, cc);
-            return;
-        }
+    const uint32_t ne = e1 - e0;
+    if (c.cta_rr == 3 && ne <= kRowBlk && (uint64_t)ne * (c.T + 1) <= 2 * kRowBlk) {
+        bitmap_row_staged(c, e0, ne, bm, sink, cc, ah);
+        return;
     }
     for (uint32_t t = 0; t < c.T; t++) {
         const uint32_t lo = t * c.tile_width;
@@ -326,10 +390,19 @@ __device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, u
         uint4* b4 = reinterpret_cast<uint4*>(bm);
         for (uint32_t w = threadIdx.x; w < words4; w += blockDim.x) b4[w] = make_uint4(0, 0, 0, 0);
         __syncthreads();
+        if (t == 0) ah.run();
         TileBitmap set{bm, lo};
-        cta_expand(c, c.JR_R[x], c.JR_R[x + 1], wib, nw_lg, t, t + 1, set, sink, cc);
+        cta_expand(c, e0, e1, wib, nw_lg, t, t + 1, set, sink, cc);
         __syncthreads();
     }
+    if (c.T == 0) ah.run();  // (every look-ahead runs once a row)
+}
+
+template <class Sink>
+__device__ __forceinline__ void single_bitmap_row(const RowCtx& c, uint32_t x, uint32_t* bm, Sink& sink,
+                                                  CtaChunks* cc) {
+    NoAhead na;
+    bitmap_row(c, c.JR_R[x], c.JR_R[x + 1], bm, sink, cc, na);
 }
 
 // ---- one join
@@ -356,16 +429,20 @@ static __global__ void __launch_bounds__(256) k_single_warp(RowCtx c, Reserve rs
 
 // Class 2: one CTA per row; 2^block_lg table words, then one staging buffer
 // per warp.
+// Rows rows[skip0 + skip1 + i], i < *nrows_p (skips: device counts, either
+// may be null), taken through row counter c.next_row[ctr].
 static __global__ void __launch_bounds__(1024) k_single_block(RowCtx c, Reserve rs, const uint32_t* __restrict__ rows,
                                                               const unsigned long long* __restrict__ nrows_p,
-                                                              uint32_t block_lg) {
+                                                              uint32_t block_lg, const unsigned long long* skip0,
+                                                              const unsigned long long* skip1, uint32_t ctr) {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_row;
     __shared__ CtaChunks s_cc;
     if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*nrows_p;
-    for (uint32_t ri = cta_next_row(&c.next_row[2], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[2], &s_row)) {
+    rows += (skip0 ? *skip0 : 0ull) + (skip1 ? *skip1 : 0ull);
+    for (uint32_t ri = cta_next_row(&c.next_row[ctr], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[ctr], &s_row)) {
         const uint32_t x = rows[ri];
         StageSink sink{stage, c.out, rs, c.id2x[x]};
         single_block_row(c, x, smem, sink, block_lg, &s_cc);
@@ -395,11 +472,17 @@ static __global__ void __launch_bounds__(DIM3G_BM_BOUNDS, DIM3G_BM_MINB) k_singl
     if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = bm + bitmap_words + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)(*n3 + *n4);
-    for (uint32_t ri = cta_next_row(&c.next_row[3], &s_row); ri < nrows; ri = cta_next_row(&c.next_row[3], &s_row)) {
-        const uint32_t x = rows[ri];
-        StageSink sink{stage, c.out, rs, c.id2x[x]};
-        single_bitmap_row(c, x, bm, sink, &s_cc);
+    __shared__ RowHead s_head[2];
+    ahead_start(c, rows, &c.next_row[3], nrows, s_head);
+    __syncthreads();
+    for (uint32_t k = 0;; k ^= 1) {
+        const RowHead h = s_head[k];
+        if (h.ri >= nrows) break;
+        RowAhead ah{&s_head[k ^ 1]};
+        StageSink sink{stage, c.out, rs, h.xv};
+        bitmap_row(c, h.e0, h.e1, bm, sink, &s_cc, ah);
         sink.flush();
+        __syncthreads();  // the next row's header is in s_head[k ^ 1]
     }
 }
 

@@ -181,6 +181,36 @@ def test_streamed_bitmap_rows_agree(built, golden, params):
     c.close()
 
 
+@pytest.mark.parametrize("split,block_lg,walk", [(1, 14, 3), (0, 14, 3), (1, 9, 3), (1, 12, 1), (1, 11, 0)])
+def test_block_split_launches_agree(built, golden, split, block_lg, walk):
+    """Block-class rows in three launches by hash-set size (block_split = 1,
+    256-thread CTAs for the two smaller sizes) or one: exact on the cases
+    with most rows in the block class (small warp sets), for several set
+    sizes and CTA walks, twice on one context (the launches' row counters
+    restart), and on the device-resident entry point."""
+    import torch
+    import dim3gpu
+    index, arrays = golden
+    c = dim3gpu.Context(0)
+    for k, v in (("block_split", split), ("warp_slots_log2", 6), ("block_slots_log2", block_lg),
+                 ("cta_walk", walk)):
+        c.set_param(k, v)
+    assert c.get_param("block_split") == split
+    for name in ["grd_small", "grd_all_dense", "grd_dense_z", "chung_lu_s005", "zipf_1m_s001", "one_join_value",
+                 "heavy_duplicates", "grd_sparse"]:
+        R, S = case_inputs(name, index, arrays)
+        for _ in range(2):
+            check_pairs(c.join_project(R, S), index[name], arrays, name)
+        dR = torch.from_numpy(R.view(np.int32)).cuda()
+        dS = torch.from_numpy(S.view(np.int32)).cuda()
+        n = index[name]["n_out"]
+        out = torch.empty((max(n, 1), 2), dtype=torch.int32, device="cuda")
+        assert c.join_project_device(dR, R.shape[0], dS, S.shape[0], out, out.shape[0]) == n
+        check_pairs(out[:n].cpu().numpy().view(np.uint32), index[name], arrays, name)
+        assert c.stats()["rows_block"] >= 0
+    c.close()
+
+
 @pytest.mark.parametrize("prefetch", [1, 0])
 def test_prefetched_block_rows_agree(built, golden, prefetch):
     """Block-class rows with their metadata fetched ahead by a producer warp
