@@ -81,17 +81,18 @@ unsigned elem_grid(uint64_t n, int sm) {
 }
 
 struct Tuning {
-    uint32_t warp_lg, block_lg, block_threads, tile_lg, cta_rr;
+    uint32_t warp_lg, block_lg, block_threads, tile_lg, cta_rr, block_split;
 };
 Tuning tuning_of(const dim3g_ctx* ctx) {
-    int64_t w = 11, b = 14, t = 512, tl = 19, rr = 2;
+    int64_t w = 11, b = 14, t = 512, tl = 19, rr = 2, bs = 1;
+    dim3g_get_param(ctx, "block_split", &bs);
     dim3g_get_param(ctx, "warp_slots_log2", &w);
     dim3g_get_param(ctx, "block_slots_log2", &b);
     dim3g_get_param(ctx, "block_threads", &t);
     dim3g_get_param(ctx, "tile_bits_log2", &tl);
     dim3g_get_param(ctx, "cta_walk", &rr);
     if (tl > 19) tl = 19;  // the batch bitmap kernel runs 512-thread CTAs
-    return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl, (uint32_t)rr};
+    return Tuning{(uint32_t)w, (uint32_t)b, (uint32_t)t, (uint32_t)tl, (uint32_t)rr, (uint32_t)bs};
 }
 
 // Warps per CTA of the warp-class kernels (about half an SM's shared memory).
@@ -366,7 +367,7 @@ struct QueryPlan {
     QueryPools Q{};
     uint32_t* lists = nullptr;             // 3 x nrows
     unsigned long long* ncls = nullptr;    // rows per class 0..8
-    uint32_t* next_row = nullptr;          // 4 dynamic counters
+    uint32_t* next_row = nullptr;          // 8 dynamic counters (4..6: split block launches)
     uint64_t* bsum = nullptr;
 };
 
@@ -391,7 +392,7 @@ QLayout query_layout(uint32_t nq, uint64_t ntot, uint64_t nrows) {
     o.rs = L.add<Reserve>(nq);
     o.res = L.add<QueryRes>(nq);
     o.lists = L.add<uint32_t>(4 * nrows);
-    o.ncls = L.add<unsigned long long>(16);
+    o.ncls = L.add<unsigned long long>(24);  // [16..18]: block-class rows by hash-set size
     o.next = L.add<uint32_t>(8);
     o.bsum = L.add<uint64_t>(scan_storage(nrows));
     o.total = L.total;
@@ -519,7 +520,7 @@ int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t
     const Tuning tu = tuning_of(ctx);
     const uint32_t nq = qp.nq;
     Q.cta_rr = tu.cta_rr;
-    BCU(cudaMemsetAsync(qp.ncls, 0, 16 * 8, st));
+    BCU(cudaMemsetAsync(qp.ncls, 0, 24 * 8, st));
     BCU(cudaMemsetAsync(Q.cls, 0, qp.nrows, st));
     BCU(cudaMemsetAsync(Q.wrow, 0, qp.nrows * 8, st));
     BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));
@@ -552,6 +553,19 @@ int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 3)}, ListDst{lm, &n[4]}, qp.nrows, qp.bsum, &n[3], st);
         device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 5)}, ListDst{lt, nullptr}, qp.nrows, qp.bsum, &n[5], st);
         launches += 5 * scan_launches(qp.nrows);
+        unsigned long long* nb = qp.ncls + 16;  // block-class rows by hash-set size (project, split)
+        const bool split = op == 0 && tu.block_split;
+        if (split) {
+            // the block rows again, ordered by hash-set size (as the single pass)
+            const uint32_t b = tu.block_lg;
+            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 0u, 1u << (b - 3)}, ListDst{lb, nullptr}, qp.nrows, qp.bsum,
+                        &nb[0], st);
+            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 1u << (b - 3), 1u << (b - 2)}, ListDst{lb, &nb[0]}, qp.nrows,
+                        qp.bsum, &nb[1], st);
+            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 1u << (b - 2), 0xFFFFFFFFu}, ListDst{lb, &nb[0], &nb[1]},
+                        qp.nrows, qp.bsum, &nb[2], st);
+            launches += 3 * scan_launches(qp.nrows);
+        }
         BCU(cudaGetLastError());
         BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));
         if (op == 0) {
@@ -560,10 +574,22 @@ int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t
                 Q, BatchRows{lm, &n[4], &n[3], &qp.next_row[0]}, bm_words);
             BLAUNCH();
             const int blk_b = (int)tu.block_threads;
-            const size_t ss_b = ((size_t)1 << tu.block_lg) * 4 + (size_t)(blk_b / 32) * kStage * 4;
-            k_b_single_block<<<resident(k_b_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(
-                Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[1]}, tu.block_lg);
-            BLAUNCH();
+            if (split) {
+                const unsigned long long* skip[3][2] = {{nullptr, nullptr}, {&nb[0], nullptr}, {&nb[0], &nb[1]}};
+                for (uint32_t k = 0; k < 3; k++) {
+                    const int thr = k < 2 ? (int)kBlockSplitThreads : blk_b;
+                    const uint32_t lg = tu.block_lg - 2 + k;
+                    const size_t ss = ((size_t)1 << lg) * 4 + (size_t)(thr / 32) * kStage * 4;
+                    k_b_single_block<<<resident(k_b_single_block, thr, ss, sm), thr, ss, st>>>(
+                        Q, BatchRows{lb, &nb[k], nullptr, &qp.next_row[4 + k], skip[k][0], skip[k][1]}, lg);
+                    BLAUNCH();
+                }
+            } else {
+                const size_t ss_b = ((size_t)1 << tu.block_lg) * 4 + (size_t)(blk_b / 32) * kStage * 4;
+                k_b_single_block<<<resident(k_b_single_block, blk_b, ss_b, sm), blk_b, ss_b, st>>>(
+                    Q, BatchRows{lb, &n[2], nullptr, &qp.next_row[1]}, tu.block_lg);
+                BLAUNCH();
+            }
             const uint32_t wps = warps_for(warp_row_words(tu.warp_lg, kStage) * 4);
             const size_t ss_w = (size_t)wps * warp_row_words(tu.warp_lg, kStage) * 4;
             k_b_single_warp<<<resident(k_b_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(

@@ -464,6 +464,11 @@ struct BatchRows {
     const unsigned long long* n_a;  // rows of the list (or its first part)
     const unsigned long long* n_b;  // second part (or nullptr)
     uint32_t* next;                 // dynamic row counter of CTA classes
+    const unsigned long long* skip0 = nullptr;  // the rows start past these counts (device; null: 0)
+    const unsigned long long* skip1 = nullptr;
+    __device__ __forceinline__ const uint32_t* rows() const {
+        return list + (skip0 ? *skip0 : 0ull) + (skip1 ? *skip1 : 0ull);
+    }
 };
 
 // ---- project, single pass: rows of many queries, each CTA (or warp) copying
@@ -498,10 +503,11 @@ static __global__ void __launch_bounds__(1024) k_b_single_block(QueryPools Q, Ba
     if (threadIdx.x == 0) s_cc.n = 0;
     uint32_t* stage = smem + (1u << block_lg) + (threadIdx.x >> 5) * kStage;
     const uint32_t nrows = (uint32_t)*L.n_a;
+    const uint32_t* rows = L.rows();
     for (uint32_t ri = cta_next_row(L.next, &s_row); ri < nrows; ri = cta_next_row(L.next, &s_row)) {
         if (threadIdx.x == 0) {
             uint32_t x;
-            s_q = query_of_row(Q, L.list[ri], &x);
+            s_q = query_of_row(Q, rows[ri], &x);
             s_x = x;
             s_c = Q.rc[s_q];
         }

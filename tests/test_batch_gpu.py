@@ -68,11 +68,13 @@ def _check(golden, specs, res):
     {},
     {"warp_slots_log2": 5, "block_slots_log2": 8, "tile_bits_log2": 10},
     {"warp_slots_log2": 8, "block_slots_log2": 10, "tile_bits_log2": 12},
+    {"warp_slots_log2": 6, "block_slots_log2": 12, "block_split": 0},
 ])
 def test_relset_golden_project_and_count(built, golden, params):
     """All golden cases as one relation set; every case's join-project and
     COUNT join-aggregate in one mixed pass (forced classes and z tilings in
-    the parametrised runs)."""
+    the parametrised runs; block-class rows in three launches by hash-set
+    size unless block_split = 0)."""
     import dim3gpu
     c = dim3gpu.Context(0)
     for k, v in params.items():
