@@ -129,6 +129,7 @@ struct dim3g_relset {
     std::vector<RelIn> h_in;
     std::vector<uint64_t> h_tup_off, h_tab_off;
     std::vector<uint64_t> h_cap;  // sketch-sized table slots per relation (when sized)
+    std::vector<uint8_t> h_roles; // CSRs each relation needs (RelRole bits; empty: both for every relation)
     bool sized = false;           // tables from h_cap (else from the tuple counts)
     uint64_t ntot = 0, tabtot = 0, yt_cap = 0;
     uint32_t tile_lg = 19;
@@ -183,7 +184,8 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
                  o_ICf = L.add<uint32_t>(s->ntot), o_ICr = L.add<uint32_t>(s->ntot), o_cyt = L.add<uint32_t>(s->yt_cap),
                  o_JRy = L.add<uint32_t>(s->yt_cap), o_curY = L.add<uint32_t>(s->yt_cap),
                  o_ICy = L.add<uint32_t>(s->ntot), o_VSy = L.add<uint32_t>(s->ntot), o_err = L.add<uint32_t>(4),
-                 o_need = L.add<unsigned long long>(2), o_yoff = L.add<uint64_t>(n + 1);
+                 o_need = L.add<unsigned long long>(2), o_yoff = L.add<uint64_t>(n + 1),
+                 o_roles = L.add<uint8_t>(n);
     uint64_t sn = scan_storage(s->tabtot);
     const uint64_t s2 = scan_storage(s->ntot + 1), s3 = scan_storage(s->yt_cap);
     if (s2 > sn) sn = s2;
@@ -231,11 +233,14 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
     P.err = (uint32_t*)(m + o_err);
     P.yt_need = (unsigned long long*)(m + o_need);
     P.yoff = (uint64_t*)(m + o_yoff);
+    P.roles = (const uint8_t*)(m + o_roles);
     s->bsum = (uint64_t*)(m + o_bsum);
     s->bsum_n = sn;
     BCU(cudaMemcpy((void*)P.in, s->h_in.data(), n * sizeof(RelIn), cudaMemcpyHostToDevice));
     BCU(cudaMemcpy((void*)P.tup_off, s->h_tup_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy((void*)P.tab_off, s->h_tab_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+    if (s->h_roles.size() != n) s->h_roles.assign(n, (uint8_t)(kRoleRows | kRoleCols));
+    BCU(cudaMemcpy((void*)P.roles, s->h_roles.data(), n, cudaMemcpyHostToDevice));
     return DIM3G_OK;
 }
 
@@ -827,6 +832,17 @@ int dim3g_batch_create(dim3g_ctx* ctx, const dim3g_relation* rels, const dim3g_q
     if (!r && (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess))
         r = I::fail(ctx, DIM3G_ERR_CUDA, "event creation failed");
     if (!r) r = set_batch_attributes(ctx);
+    if (!r) {
+        // each relation of a batch has one role: the relation that drives its
+        // join (the larger, as query_plan swaps) needs only its CSR by first
+        // value, the other only its CSR by (y, z tile)
+        b->set.h_roles.assign(2 * (size_t)n, 0);
+        for (uint32_t i = 0; i < n; i++) {
+            const bool sw = rels[2 * i].n < rels[2 * i + 1].n;
+            b->set.h_roles[2 * i + (sw ? 1 : 0)] |= kRoleRows;
+            b->set.h_roles[2 * i + (sw ? 0 : 1)] |= kRoleCols;
+        }
+    }
     if (!r) r = relset_sketch(&b->set, b->rels.data(), 2 * n);
     if (!r) r = relset_plan(&b->set, b->rels.data(), 2 * n, 0);
     if (!r) r = query_plan(&b->set, b->set.qs, b->queries.data(), n, b->qp);

@@ -97,6 +97,11 @@ struct RelDev {
     uint32_t probe_lim; // longest probe of the tables (0: the whole table)
 };
 
+// The CSRs a relation's queries read: kRoleRows, by first value (the
+// relation drives the rows of a join); kRoleCols, by (y, z tile) (its first
+// values are a join's output column).
+enum RelRole : uint8_t { kRoleRows = 1, kRoleCols = 2 };
+
 // Pools of one relation set (device pointers).
 struct RelPools {
     const RelIn* in;
@@ -127,6 +132,7 @@ struct RelPools {
     uint32_t* err;            // device error flags of the set
     unsigned long long* yt_need;  // keys the layout needs (+1)
     uint64_t* yoff;           // nrel + 1: first global y id of each relation
+    const uint8_t* roles;     // nrel: RelRole bits (CSRs built for the relation)
 };
 
 __device__ __forceinline__ DevTable rel_table(unsigned long long* pool, const RelDev& r) {
@@ -214,6 +220,11 @@ static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t 
             d.probe_lim = P.probe_lim;
             P.rel[r] = d;
             P.yoff[r] = d.ybase;
+            // a relation without the by-first-value CSR still takes its
+            // tuples' positions in that CSR's global prefix (at its first
+            // id, in one add), so every relation's positions stay
+            // [tup_off, tup_off + nt) for the ones that have it
+            if (!(P.roles[r] & kRoleRows) && d.nt) atomicAdd(&P.degF[d.fbase], (uint32_t)d.nt);
         }
         cf += tf;
         cy += ty;
@@ -241,9 +252,12 @@ static __global__ void k_ix_map(RelPools P) {
         const uint32_t fid = table_find(rel_table(P.TF, d), t.x);
         const uint32_t yid = table_find(rel_table(P.TY, d), t.y);
         P.Pm[i] = make_uint2(fid, yid);
-        atomicAdd(&P.degF[fid], 1u);
-        const uint64_t key = d.yt_base + (uint64_t)(yid - d.ybase) * d.T + ((fid - d.fbase) >> d.tile_shift);
-        atomic_inc_agg(P.cnt_yt, key);  // heavy y keys repeat within a warp
+        const uint8_t ro = P.roles[r];
+        if (ro & kRoleRows) atomicAdd(&P.degF[fid], 1u);
+        if (ro & kRoleCols) {
+            const uint64_t key = d.yt_base + (uint64_t)(yid - d.ybase) * d.T + ((fid - d.fbase) >> d.tile_shift);
+            atomic_inc_agg(P.cnt_yt, key);  // heavy y keys repeat within a warp
+        }
     }
 }
 
@@ -254,14 +268,19 @@ static __global__ void k_ix_scatter(RelPools P) {
         const uint32_t r = sc.at(i);
         const RelDev& d = P.rel[r];
         const uint2 pm = P.Pm[i];
-        const uint32_t pos = atomicAdd(&P.curF[pm.x], 1u);
-        P.ICf[pos] = pm.y;
-        P.ICr[pos] = pm.x - (uint32_t)d.fbase;
+        const uint8_t ro = P.roles[r];
         const uint32_t fl = pm.x - (uint32_t)d.fbase;
-        const uint64_t key = d.yt_base + (uint64_t)(pm.y - d.ybase) * d.T + (fl >> d.tile_shift);
-        const uint32_t p2 = atomic_inc_agg(P.curY, key);
-        P.ICy[p2] = fl;
-        P.VSy[p2] = P.in[r].pairs[i - sc.lo].x;
+        if (ro & kRoleRows) {
+            const uint32_t pos = atomicAdd(&P.curF[pm.x], 1u);
+            P.ICf[pos] = pm.y;
+            P.ICr[pos] = fl;
+        }
+        if (ro & kRoleCols) {
+            const uint64_t key = d.yt_base + (uint64_t)(pm.y - d.ybase) * d.T + (fl >> d.tile_shift);
+            const uint32_t p2 = atomic_inc_agg(P.curY, key);
+            P.ICy[p2] = fl;
+            P.VSy[p2] = P.in[r].pairs[i - sc.lo].x;
+        }
     }
 }
 

@@ -139,6 +139,8 @@ struct dim3g_ctx {
     void* d_sum = nullptr;  // per-A-tile summary accumulators
     size_t d_sum_bytes = 0;
     Scalars* h_sc = nullptr;  // pinned
+    cudaStream_t aux = nullptr;  // side stream: R's CSR build alongside S's (fork/join by events)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev[6] = {};
     cudaEvent_t evc[8] = {};  // per row-class kernel timing
     cudaEvent_t evd[4] = {};  // dense block: selection, operands, product, light pass
@@ -179,8 +181,9 @@ int fail(dim3g_ctx* c, int code, const char* fmt, ...) {
 
 // device_scan plus launch accounting (three kernels when n > 0).
 template <class Src, class Dst>
-int run_scan(dim3g_ctx* c, Src src, Dst dst, uint64_t n, uint64_t* bsum, unsigned long long* total) {
-    device_scan(src, dst, n, bsum, total, c->stream);
+int run_scan(dim3g_ctx* c, Src src, Dst dst, uint64_t n, uint64_t* bsum, unsigned long long* total,
+             cudaStream_t on = nullptr) {
+    device_scan(src, dst, n, bsum, total, on ? on : c->stream);
     CU(cudaGetLastError());
     c->launches += scan_launches(n);
     return DIM3G_OK;
@@ -696,22 +699,34 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
     uint32_t* cnt = ws_get<uint32_t>(c, (uint64_t)n + 1);  // cnt[n] = 0 closes the offsets scan
     unsigned long long* off = ws_get<unsigned long long>(c, (uint64_t)n + 1);
     uint64_t* bsum2 = ws_get<uint64_t>(c, scan_storage((nyt > n ? nyt : n) + 1));
+    uint64_t* bsum_r = ws_get<uint64_t>(c, scan_storage((uint64_t)n + 1));
     if (!degx || !curx || !JR_R || !IC_R || !cnt_yt || !cur_yt || !JR_S || !IC_S || !ISV || !Zq || !ucap || !cls || !lists ||
-        !cnt || !off || !bsum2)
+        !cnt || !off || !bsum2 || !bsum_r)
         return fail(c, DIM3G_ERR_NOMEM, "workspace allocation failed (CSR)");
 
-    CU(cudaMemsetAsync(degx, 0, ((uint64_t)n + 1) * 4, st));
+    // The two CSRs are independent: R's (by x) on the side stream while S's
+    // (by (y, z tile)) runs here; both are latency-bound scatters, so they
+    // overlap.  Joined before the row classification.
+    const cudaStream_t ax = c->aux;
+    CU(cudaEventRecord(c->ev_fork, st));
+    CU(cudaStreamWaitEvent(ax, c->ev_fork, 0));
+    CU(cudaMemsetAsync(degx, 0, ((uint64_t)n + 1) * 4, ax));
+    k_map_p<<<grid_for(jp.nP, sm), 256, 0, ax>>>(jp.P, jp.nP, tx, ty, Pm, degx);
+    CHECK_LAUNCH();
+    {
+        int r = run_scan(c, U32Src{degx}, RowPtrDst{JR_R, curx}, (uint64_t)n + 1, bsum_r, nullptr, ax);
+        if (r) return r;
+    }
+    k_scatter_r<<<grid_for(jp.nP, sm), 256, 0, ax>>>(Pm, jp.nP, curx, IC_R);
+    CHECK_LAUNCH();
+    CU(cudaEventRecord(c->ev_join, ax));
     CU(cudaMemsetAsync(cnt_yt, 0, (nyt + 1) * 4, st));
-    k_map_p<<<grid_for(jp.nP, sm), 256, 0, st>>>(jp.P, jp.nP, tx, ty, Pm, degx);
-    CHECK_LAUNCH();
     k_map_q<<<grid_for(nq, sm), 256, 0, st>>>(Qk, nq, tz, T, tile_shift, Zq, cnt_yt);
-    CHECK_LAUNCH();
-    SCAN(U32Src{degx}, RowPtrDst{JR_R, curx}, (uint64_t)n + 1, bsum2, nullptr);
-    k_scatter_r<<<grid_for(jp.nP, sm), 256, 0, st>>>(Pm, jp.nP, curx, IC_R);
     CHECK_LAUNCH();
     SCAN(U32Src{cnt_yt}, RowPtrDst{JR_S, cur_yt}, nyt + 1, bsum2, nullptr);
     k_scatter_s<<<grid_for(nq, sm), 256, 0, st>>>(Qk, Zq, nq, T, tile_shift, cur_yt, IC_S, VS, ISV);
     CHECK_LAUNCH();
+    CU(cudaStreamWaitEvent(st, c->ev_join, 0));
 
     RowCtx rc{};
     rc.JR_R = JR_R;
@@ -1210,6 +1225,9 @@ int dim3g_create(int device, dim3g_ctx** out) {
     dim3g_ctx* c = new dim3g_ctx();
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_sc, sizeof(Scalars)) != cudaSuccess) {
         cudaGetLastError();
@@ -1272,6 +1290,9 @@ void dim3g_destroy(dim3g_ctx* c) {
         if (e) cudaEventDestroy(e);
     for (auto& e : c->evd)
         if (e) cudaEventDestroy(e);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }

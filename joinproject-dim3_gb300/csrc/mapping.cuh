@@ -196,7 +196,7 @@ static __global__ void k_map_q(const uint2* __restrict__ Qk, uint64_t n, DevTabl
         uint2 q = Qk[i];
         uint32_t zi = table_find(tz, q.x);
         zid[i] = zi;
-        atomic_inc_agg(cnt_yt, (uint64_t)q.y * T + (zi >> tile_shift));  // skewed y repeat within a warp
+        atomicAdd(&cnt_yt[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
     }
 }
 
@@ -234,7 +234,7 @@ static __global__ void k_scatter_s(const uint2* __restrict__ Qk, const uint32_t*
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint2 q = Qk[i];
         uint32_t zi = zid[i];
-        uint32_t pos = atomic_inc_agg(cursor, (uint64_t)q.y * T + (zi >> tile_shift));
+        uint32_t pos = atomicAdd(&cursor[(uint64_t)q.y * T + (zi >> tile_shift)], 1u);
         ic[pos] = zi;
         if (vs) vs[pos] = q.x;
         if (isv) isv[pos] = make_uint2(zi, q.x);
