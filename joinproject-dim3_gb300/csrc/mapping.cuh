@@ -86,7 +86,7 @@ inline uint64_t next_pow2(uint64_t v) {
 // (most updates once the registers have filled).
 __device__ __forceinline__ void sketch_add_if_larger(uint32_t* r, uint32_t key) {
     const uint2 s = sketch_slot(key);
-    if (__ldcg(&r[s.x]) < s.y) atomicMax(&r[s.x], s.y);
+    if (*(volatile uint32_t*)&r[s.x] < s.y) atomicMax(&r[s.x], s.y);
 }
 
 // HyperLogLog estimate (with the small-range correction) from a column's
@@ -113,11 +113,11 @@ static __global__ void __launch_bounds__(256) k_sketch(const uint2* __restrict__
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nP; i += stride) {
         const uint2 p = P[i];
-        sketch_add(r, p.x);
-        sketch_add(r + kSketchRegs, p.y);
+        sketch_add_if_larger(r, p.x);
+        sketch_add_if_larger(r + kSketchRegs, p.y);
     }
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nQ; i += stride)
-        sketch_add(r + 2 * kSketchRegs, Q[i].x);
+        sketch_add_if_larger(r + 2 * kSketchRegs, Q[i].x);
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < 3 * kSketchRegs; k += blockDim.x)
         if (r[k]) atomicMax(&regs[k], r[k]);
