@@ -185,7 +185,7 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
                  o_JRy = L.add<uint32_t>(s->yt_cap), o_curY = L.add<uint32_t>(s->yt_cap),
                  o_ICy = L.add<uint32_t>(s->ntot), o_VSy = L.add<uint32_t>(s->ntot), o_err = L.add<uint32_t>(4),
                  o_need = L.add<unsigned long long>(2), o_yoff = L.add<uint64_t>(n + 1),
-                 o_roles = L.add<uint8_t>(n);
+                 o_roles = L.add<uint8_t>(n), o_fneed = L.add<unsigned long long>(1);
     uint64_t sn = scan_storage(s->tabtot);
     const uint64_t s2 = scan_storage(s->ntot + 1), s3 = scan_storage(s->yt_cap);
     if (s2 > sn) sn = s2;
@@ -234,6 +234,7 @@ int relset_plan(dim3g_relset* s, const dim3g_relation* rels, uint32_t n, uint64_
     P.yt_need = (unsigned long long*)(m + o_need);
     P.yoff = (uint64_t*)(m + o_yoff);
     P.roles = (const uint8_t*)(m + o_roles);
+    P.f_need = (unsigned long long*)(m + o_fneed);
     s->bsum = (uint64_t*)(m + o_bsum);
     s->bsum_n = sn;
     BCU(cudaMemcpy((void*)P.in, s->h_in.data(), n * sizeof(RelIn), cudaMemcpyHostToDevice));
@@ -347,9 +348,13 @@ int relset_enqueue_build(dim3g_relset* s, cudaStream_t st, uint64_t& launches) {
         k_ix_map<<<elem_grid(s->ntot, sm), 256, 0, st>>>(P);
         BLAUNCH();
     }
-    device_scan(U32Src{P.degF}, RowPtrDst{P.JRf, P.curF}, s->ntot + 1, s->bsum, nullptr, st);
+    // row pointers up to the id / key counts the layout found (the launch
+    // covers the tuple-count bounds; past the counts nothing is read or written)
+    device_scan(BoundSrc<U32Src>{U32Src{P.degF}, P.f_need}, BoundDst<RowPtrDst>{RowPtrDst{P.JRf, P.curF}, P.f_need},
+                s->ntot + 1, s->bsum, nullptr, st);
     launches += scan_launches(s->ntot + 1);
-    device_scan(U32Src{P.cnt_yt}, RowPtrDst{P.JRy, P.curY}, s->yt_cap, s->bsum, nullptr, st);
+    device_scan(BoundSrc<U32Src>{U32Src{P.cnt_yt}, P.yt_need}, BoundDst<RowPtrDst>{RowPtrDst{P.JRy, P.curY}, P.yt_need},
+                s->yt_cap, s->bsum, nullptr, st);
     launches += scan_launches(s->yt_cap);
     BCU(cudaGetLastError());
     if (s->ntot) {
@@ -374,12 +379,14 @@ struct QueryPlan {
     unsigned long long* ncls = nullptr;    // rows per class 0..8
     uint32_t* next_row = nullptr;          // 8 dynamic counters (4..6: split block launches)
     uint64_t* bsum = nullptr;
+    uint32_t* part = nullptr;              // class-list partition: per-tile bucket offsets
+    unsigned long long* pbase = nullptr;   // its bucket starts (8)
 };
 
 // Device layout of a query pass's scratch (every size monotone in the
 // arguments, so scratch laid out for maxima fits every smaller pass).
 struct QLayout {
-    size_t qin, qt, qr, ymap, ICq, JRq, ucap, cls, wrow, rc, rs, res, lists, ncls, next, bsum, total;
+    size_t qin, qt, qr, ymap, ICq, JRq, ucap, cls, wrow, rc, rs, res, lists, ncls, next, bsum, part, pbase, total;
 };
 QLayout query_layout(uint32_t nq, uint64_t ntot, uint64_t nrows) {
     Layout L;
@@ -400,6 +407,8 @@ QLayout query_layout(uint32_t nq, uint64_t ntot, uint64_t nrows) {
     o.ncls = L.add<unsigned long long>(24);  // [16..18]: block-class rows by hash-set size
     o.next = L.add<uint32_t>(8);
     o.bsum = L.add<uint64_t>(scan_storage(nrows));
+    o.part = L.add<uint32_t>(8 * ((nrows + kPartTile - 1) / kPartTile));
+    o.pbase = L.add<unsigned long long>(8);
     o.total = L.total;
     return o;
 }
@@ -500,6 +509,8 @@ int query_plan(dim3g_relset* s, QueryScratch& qs, const dim3g_query* q, uint32_t
     qp.ncls = (unsigned long long*)(m + o.ncls);
     qp.next_row = (uint32_t*)(m + o.next);
     qp.bsum = (uint64_t*)(m + o.bsum);
+    qp.part = (uint32_t*)(m + o.part);
+    qp.pbase = (unsigned long long*)(m + o.pbase);
     return DIM3G_OK;
 }
 
@@ -552,24 +563,22 @@ int query_enqueue(dim3g_relset* s, QueryScratch& qs, QueryPlan& qp, cudaStream_t
         if (op == 1 && !qp.has_count) continue;
         const uint8_t k0 = op ? 8 : 0;
         unsigned long long* n = qp.ncls + 8 * op;  // n[1..5]: rows of classes k0+1..k0+5
-        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 1)}, ListDst{lw, nullptr}, qp.nrows, qp.bsum, &n[1], st);
-        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 2)}, ListDst{lb, nullptr}, qp.nrows, qp.bsum, &n[2], st);
-        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 4)}, ListDst{lm, nullptr}, qp.nrows, qp.bsum, &n[4], st);
-        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 3)}, ListDst{lm, &n[4]}, qp.nrows, qp.bsum, &n[3], st);
-        device_scan(ClassSrc{Q.cls, (uint8_t)(k0 + 5)}, ListDst{lt, nullptr}, qp.nrows, qp.bsum, &n[5], st);
-        launches += 5 * scan_launches(qp.nrows);
         unsigned long long* nb = qp.ncls + 16;  // block-class rows by hash-set size (project, split)
         const bool split = op == 0 && tu.block_split;
-        if (split) {
-            // the block rows again, ordered by hash-set size (as the single pass)
+        {
+            // the class lists (and the CTA class by hash-set size) in one partition
             const uint32_t b = tu.block_lg;
-            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 0u, 1u << (b - 3)}, ListDst{lb, nullptr}, qp.nrows, qp.bsum,
-                        &nb[0], st);
-            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 1u << (b - 3), 1u << (b - 2)}, ListDst{lb, &nb[0]}, qp.nrows,
-                        qp.bsum, &nb[1], st);
-            device_scan(BlockSizeSrc{Q.cls, Q.ucap, 1u << (b - 2), 0xFFFFFFFFu}, ListDst{lb, &nb[0], &nb[1]},
-                        qp.nrows, qp.bsum, &nb[2], st);
-            launches += 3 * scan_launches(qp.nrows);
+            const PartSpec ps{k0, split ? 1u : 0u, 1u << (b - 3), 1u << (b - 2)};
+            const uint64_t ntiles = (qp.nrows + kPartTile - 1) / kPartTile;
+            if (ntiles) {
+                k_part_count<<<(unsigned)ntiles, 256, 0, st>>>(Q.cls, Q.ucap, qp.nrows, ps, qp.part);
+                BLAUNCH();
+                k_part_offsets<<<1, 1024, 0, st>>>(qp.part, (uint32_t)ntiles, n, split ? nb : nullptr, qp.pbase);
+                BLAUNCH();
+                k_part_scatter<<<(unsigned)ntiles, 256, 0, st>>>(Q.cls, Q.ucap, qp.nrows, ps, qp.part, qp.pbase, lw, lb,
+                                                                 lm, lt);
+                BLAUNCH();
+            }
         }
         BCU(cudaGetLastError());
         BCU(cudaMemsetAsync(qp.next_row, 0, 8 * 4, st));

@@ -131,6 +131,7 @@ struct RelPools {
     uint32_t* VSy;            // f values
     uint32_t* err;            // device error flags of the set
     unsigned long long* yt_need;  // keys the layout needs (+1)
+    unsigned long long* f_need;   // first-value ids of the set (+1): the by-first-value row pointers scanned
     uint64_t* yoff;           // nrel + 1: first global y id of each relation
     const uint8_t* roles;     // nrel: RelRole bits (CSRs built for the relation)
 };
@@ -232,6 +233,7 @@ static __global__ void __launch_bounds__(1024) k_ix_layout(RelPools P, uint32_t 
     }
     if (threadIdx.x == 0) {
         P.yoff[P.nrel] = cy;
+        *P.f_need = cf + 1;
         *P.yt_need = ck + 1;
         if (ck + 1 > P.yt_cap) raise_error(P.err, kErrTableFull);
         // a sketch-sized table overflowed its probe bound: some ids are
@@ -468,6 +470,137 @@ static __global__ void k_q_row_work(QueryPools Q, uint32_t cap_w, uint32_t cap_b
         }
         Q.cls[g] = (uint8_t)k;
         atomic_add_grouped(&Q.res[qi].out_j, qi, w);  // one atomic per query run
+    }
+}
+
+// ---- class lists in one partition of the row space (instead of one
+// prefix sum per class).  A row's bucket: 0 warp class (k0+1); 1..3 CTA
+// class (k0+2), by distinct bound u <= capS, u <= capM, larger when split
+// (else all 1); 4 huge bitmap rows (k0+4); 5 bitmap rows (k0+3); 6 tiny
+// rows (k0+5); 7 none.  Three launches: per-tile bucket counts, their
+// prefix per bucket (one CTA), the scatter into the lists.  Order within a
+// list is unspecified (rows are claimed dynamically anyway).
+constexpr uint32_t kPartItems = 16;
+constexpr uint32_t kPartTile = 256 * kPartItems;  // rows a CTA tile
+constexpr uint32_t kPartBuckets = 7;
+struct PartSpec {
+    uint32_t k0, split, capS, capM;
+};
+__device__ __forceinline__ uint32_t row_bucket(const uint8_t* __restrict__ cls, const uint32_t* __restrict__ ucap,
+                                               uint64_t i, const PartSpec& ps) {
+    const uint32_t c = cls[i];
+    if (c == ps.k0 + 1u) return 0;
+    if (c == ps.k0 + 2u) {
+        if (!ps.split) return 1;
+        const uint32_t u = ucap[i];
+        return u <= ps.capS ? 1u : (u <= ps.capM ? 2u : 3u);
+    }
+    if (c == ps.k0 + 4u) return 4;
+    if (c == ps.k0 + 3u) return 5;
+    if (c == ps.k0 + 5u) return 6;
+    return 7;
+}
+
+// hist[tile * 8 + b] = rows of bucket b in the tile.
+static __global__ void __launch_bounds__(256) k_part_count(const uint8_t* __restrict__ cls,
+                                                           const uint32_t* __restrict__ ucap, uint64_t n, PartSpec ps,
+                                                           uint32_t* __restrict__ hist) {
+    __shared__ uint32_t s[8];
+    if (threadIdx.x < 8) s[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * kPartTile;
+    uint32_t c[kPartBuckets];
+#pragma unroll
+    for (uint32_t b = 0; b < kPartBuckets; b++) c[b] = 0;
+#pragma unroll 4
+    for (uint32_t k = 0; k < kPartItems; k++) {
+        const uint64_t i = base + (uint64_t)k * 256 + threadIdx.x;
+        const uint32_t b = i < n ? row_bucket(cls, ucap, i, ps) : 7u;
+#pragma unroll
+        for (uint32_t q = 0; q < kPartBuckets; q++) c[q] += b == q ? 1u : 0u;
+    }
+#pragma unroll
+    for (uint32_t q = 0; q < kPartBuckets; q++) {
+        const uint32_t v = warp_sum(c[q]);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s[q], v);
+    }
+    __syncthreads();
+    if (threadIdx.x < kPartBuckets) hist[(uint64_t)blockIdx.x * 8 + threadIdx.x] = s[threadIdx.x];
+}
+
+// One CTA: hist becomes each tile's first position in its bucket; the
+// bucket totals go to the class counts (n[1..5] as the class prefix sums
+// gave them; nb[0..2] the split CTA class), base[b] = where bucket b starts
+// in its list.
+static __global__ void __launch_bounds__(1024) k_part_offsets(uint32_t* __restrict__ hist, uint32_t ntiles,
+                                                              unsigned long long* n, unsigned long long* nb,
+                                                              unsigned long long* base) {
+    __shared__ uint64_t sm[1024 / 32 + 1];
+    __shared__ unsigned long long tot[8];
+    for (uint32_t b = 0; b < kPartBuckets; b++) {
+        uint64_t carry = 0;
+        for (uint32_t t0 = 0; t0 < ntiles; t0 += 1024) {
+            const uint32_t t = t0 + threadIdx.x;
+            const uint64_t v = t < ntiles ? hist[(uint64_t)t * 8 + b] : 0u;
+            uint64_t sum;
+            const uint64_t e = block_excl_scan<1024>(v, sm, &sum);
+            if (t < ntiles) hist[(uint64_t)t * 8 + b] = (uint32_t)(carry + e);
+            carry += sum;
+        }
+        if (threadIdx.x == 0) tot[b] = carry;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        n[1] = tot[0];
+        n[2] = tot[1] + tot[2] + tot[3];
+        if (nb) {
+            nb[0] = tot[1];
+            nb[1] = tot[2];
+            nb[2] = tot[3];
+        }
+        n[4] = tot[4];
+        n[3] = tot[5];
+        n[5] = tot[6];
+        base[0] = 0;
+        base[1] = 0;
+        base[2] = tot[1];
+        base[3] = tot[1] + tot[2];
+        base[4] = 0;
+        base[5] = tot[4];
+        base[6] = 0;
+    }
+}
+
+// Each row of a bucket to list[base[b] + its tile's offset + its rank in the
+// tile] (one shared atomic per group of lanes with the same bucket).
+static __global__ void __launch_bounds__(256) k_part_scatter(const uint8_t* __restrict__ cls,
+                                                             const uint32_t* __restrict__ ucap, uint64_t n,
+                                                             PartSpec ps, const uint32_t* __restrict__ off,
+                                                             const unsigned long long* __restrict__ base,
+                                                             uint32_t* lw, uint32_t* lb, uint32_t* lm,
+                                                             uint32_t* lt) {
+    __shared__ uint32_t s[8];
+    __shared__ unsigned long long s_at[8];
+    if (threadIdx.x < kPartBuckets) {
+        s[threadIdx.x] = 0;
+        s_at[threadIdx.x] = base[threadIdx.x] + off[(uint64_t)blockIdx.x * 8 + threadIdx.x];
+    }
+    __syncthreads();
+    const uint64_t t0 = (uint64_t)blockIdx.x * kPartTile;
+    const uint32_t lane = lane_id();
+    for (uint32_t k = 0; k < kPartItems; k++) {
+        const uint64_t i = t0 + (uint64_t)k * 256 + threadIdx.x;
+        const uint32_t b = i < n ? row_bucket(cls, ucap, i, ps) : 7u;
+        const unsigned grp = __match_any_sync(0xffffffffu, b);
+        const int leader = __ffs(grp) - 1;
+        uint32_t r0 = 0;
+        if ((int)lane == leader && b < kPartBuckets) r0 = atomicAdd(&s[b], (uint32_t)__popc(grp));
+        r0 = __shfl_sync(0xffffffffu, r0, leader);
+        if (b < kPartBuckets) {
+            const unsigned long long pos = s_at[b] + r0 + __popc(grp & lanemask_lt());
+            uint32_t* list = b == 0 ? lw : (b <= 3 ? lb : (b <= 5 ? lm : lt));
+            list[pos] = (uint32_t)i;
+        }
     }
 }
 

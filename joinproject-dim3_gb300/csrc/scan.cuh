@@ -109,6 +109,24 @@ struct SumsDst {
     __device__ void operator()(uint64_t i, uint64_t e, uint64_t) const { a[i] = e; }
 };
 
+// A scan whose length is only known on the device: items at or past *lim
+// count as 0 and are neither read nor written (the launch still covers the
+// host's upper bound n, and blocks past the limit do no memory traffic).
+template <class Src>
+struct BoundSrc {
+    Src s;
+    const unsigned long long* lim;
+    __device__ uint64_t operator()(uint64_t i) const { return i < *lim ? s(i) : 0u; }
+};
+template <class Dst>
+struct BoundDst {
+    Dst d;
+    const unsigned long long* lim;
+    __device__ void operator()(uint64_t i, uint64_t e, uint64_t v) const {
+        if (i < *lim) d(i, e, v);
+    }
+};
+
 template <class Src, class Dst>
 inline void device_scan(Src src, Dst dst, uint64_t n, uint64_t* block_sums, unsigned long long* total, cudaStream_t st);
 
