@@ -104,6 +104,7 @@ struct Params {
 };
 
 constexpr size_t kMaxSmemOptin = 227 * 1024;  // dynamic shared memory a CTA may opt into
+constexpr uint32_t kFlatAvgBitmap = 160, kFlatAvgBlock = 560, kFlatAvgWarp = 160;  // single pass, per row class
 constexpr uint32_t kAggTileLg = 15;  // join-aggregate class-3 tile: 32K counters (128 KB)
 
 struct Scalars {
@@ -858,6 +859,10 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
                 list_m, dp.nd, dp.D, dp.Wd, dp.Wm, dp.cpr, dp.coff, id2x, id2z, out, nullptr, &sc->dense_base);
             CHECK_LAUNCH();
         }
+        // the cross-segment gather's threshold per row class, measured on
+        // the 2-hop (bitmap rows 45.5 -> 44.7 ms at 160, block rows 26.3 ->
+        // 25.7 at 560, warp rows 2.62 -> 2.58 at 160; every setting exact)
+        rc.flat_avg = kFlatAvgBitmap;
         if (c->prm.stream_rows && stream_smem_bytes(bm_words) <= kMaxSmemOptin) {
             const size_t ss_s = stream_smem_bytes(bm_words);
             k_stream_bitmap<<<resident_grid(k_stream_bitmap, kStreamThreads, ss_s, sm), kStreamThreads, ss_s, st>>>(
@@ -869,6 +874,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[5], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[0], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
+        rc.flat_avg = kFlatAvgBlock;
         if (c->prm.prefetch_rows && c->prm.cta_rr == 3) {
             const size_t ss_p = (((size_t)1 << c->prm.block_lg) + (size_t)kPfWorkers * kStage) * 4;
             k_single_block_pf<<<resident_grid(k_single_block_pf, kPfThreads, ss_p, sm), kPfThreads, ss_p, st>>>(
@@ -893,6 +899,7 @@ int run_join(dim3g_ctx* c, const JoinPlan& jp, uint64_t* n_out) {
         CHECK_LAUNCH();
         CU(cudaEventRecord(c->evc[6], st));
         CU(cudaMemcpyAsync(&sc->cursor_at[1], &sc->cursor, 8, cudaMemcpyDeviceToDevice, st));
+        rc.flat_avg = kFlatAvgWarp;
         k_single_warp<<<resident_grid(k_single_warp, 32 * wps, ss_w, sm), 32 * wps, ss_w, st>>>(rc, rs, L.w, L.nw,
                                                                                            c->prm.warp_lg, kStage);
         CHECK_LAUNCH();

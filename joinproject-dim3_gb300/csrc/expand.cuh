@@ -66,6 +66,7 @@ struct RowCtx {
     uint32_t tile_width;   // z ids per tile (bitmap width)
     uint32_t m;            // z domain size
     uint32_t cta_rr;       // CTA rows' walk: 0 flattened, 1 chunks round-robin, 2 chunks split, 3 balanced (cta_expand)
+    uint32_t flat_avg;     // cross-segment gather below this many candidates a segment (0: kFlatAvgMax)
     const uint32_t* ucap;  // per row min(candidates, m)
     uint32_t* cnt;         // per row distinct count (count pass output)
     const unsigned long long* off;  // per row output offset (write pass input)
@@ -110,7 +111,8 @@ __device__ __forceinline__ bool smem_set_insert(uint32_t* tab, uint32_t lg, uint
 constexpr uint32_t kUnroll = DIM3G_UNROLL;
 constexpr uint32_t kMinPiece = DIM3G_MIN_PIECE;
 // A chunk whose segments average fewer candidates than this is gathered
-// across segment boundaries (see warp_expand).
+// across segment boundaries (see warp_expand); RowCtx::flat_avg overrides it
+// per launch (the single pass sets it per row class).
 constexpr uint32_t kFlatAvgMax = DIM3G_FLAT_AVG;
 
 // Warp-level expansion of the candidates of R entries [e0, e1) over S tiles
@@ -183,7 +185,7 @@ __device__ __forceinline__ void expand_piece_impl(const RowCtx& c, const Chunk& 
                                                   Set& set, Sink& sink, uint64_t pol) {
     const uint32_t lane = lane_id();
     const uint32_t nseg = __popc(__ballot_sync(0xffffffffu, ch.len != 0));
-    if (ch.total < kFlatAvgMax * nseg) {
+    if (ch.total < (c.flat_avg ? c.flat_avg : kFlatAvgMax) * nseg) {
         for (uint32_t cb = p0; cb < p1; cb += 32 * kUnroll) {
             uint32_t z[kUnroll], v[kUnroll];
 #pragma unroll
