@@ -315,7 +315,12 @@ int relset_sketch(dim3g_relset* s, const dim3g_relation* rels, uint32_t n) {
 // true when the set was re-planned with tuple-sized tables (build again).
 bool relset_unsize(dim3g_relset* s, const dim3g_relation* rels, int* rc) {
     *rc = DIM3G_OK;
-    if (!s->sized || !((uint32_t)s->h_need[1] & kErrProbeLimit)) return false;
+    if (!((uint32_t)s->h_need[1] & kErrProbeLimit)) return false;
+    if (!s->sized) {
+        // a tuple-sized table (twice the tuples) cannot fill: a device fault
+        *rc = I::fail(s->ctx, DIM3G_ERR_DEVICE, "relation set build: a tuple-sized table overflowed");
+        return true;
+    }
     s->sized = false;
     *rc = relset_plan(s, rels, s->nrel, s->yt_cap);
     return true;
