@@ -1,7 +1,8 @@
 """GPU tests of the serving loop (dim3g_server_*): requests submitted
 concurrently from several threads give, each, exactly the result the same
-join gives alone (golden fixtures, or a one-query pass over the set), under
-a budget that forces admission to wait; the pair matrix is exact."""
+join gives alone (a one-query pass over the set, itself checked against the
+oracle on the same relations), under a budget that forces admission to
+wait; the pair matrix is exact."""
 import threading
 
 import numpy as np
@@ -91,6 +92,20 @@ def test_served_results_equal_alone(ctx, golden, lanes, budget_mb):
     want = {}
     for r, s, op in set(reqs):
         want[(r, s, op)] = _canon(*_alone(rs, r, s, op))
+    # the one-query passes the served results are held to are themselves
+    # checked against the oracle on the same relations (its swap rule
+    # orients the pairs as the set's does)
+    from oracle import oracle_py as O
+    for (r, s, op), (wk, wc) in want.items():
+        if op == dim3gpu.OP_PROJECT:
+            wp, _, _, _ = O.join_project(host[r], host[s])
+            assert np.array_equal(wk, np.sort(O.pair_keys(wp))), (r, s, op)
+        else:
+            wg, wcnt, _, _, _ = O.join_count(host[r], host[s])
+            k = O.pair_keys(wg)
+            o = np.argsort(k)
+            assert np.array_equal(wk, k[o]), (r, s, op)
+            assert np.array_equal(wc, np.asarray(wcnt, dtype=np.uint64)[o]), (r, s, op)
     m = rs.pair_outj()
     largest = max(((int(m[r, s]) * 8 + 255) // 256) * 256 * 2 for r, s, _ in reqs)  # a COUNT reservation bound
     if budget_mb == 0:
