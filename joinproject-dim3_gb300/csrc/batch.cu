@@ -2,18 +2,22 @@
 // independent joins run as one CUDA graph, and a serving loop with
 // continuous batching over a resident set (host side; kernels in batch.cuh).
 //
+// Relation set creation: a distinct-key sketch of every relation's columns
+// sizes its value -> id tables (k_rel_sketch, synchronised once).
 // Relation set build (one stream, no host synchronisation inside):
 //   memsets -> k_ix_insert -> k_ix_layout -> id scans (TF, TY) -> k_ix_map
-//   -> CSR scans (by f, by (y, f tile)) -> k_ix_scatter
+//   -> CSR scans (by f, by (y, f tile); bounded by the layout's counts)
+//   -> k_ix_scatter (a batch builds only the CSR each relation's query reads)
 // Query pass over queries (P, Q) of a set:
 //   k_q_setup -> k_q_ymap -> k_q_entries -> k_q_rows -> k_q_row_work
-//   -> class lists (prefix sums) -> project row kernels -> COUNT row kernels
-//   -> per-query results to pinned host memory
+//   -> class lists (one partition) -> project row kernels -> COUNT row
+//   kernels -> per-query results to pinned host memory
 // Every size the launches depend on is known on the host from the tuple
 // counts; counts that depend on the data (distinct values, rows per class,
-// output sizes) stay on the device.  The one data-dependent bound, the
-// (y, f tile) key space, is checked on the device; on overflow the host
-// regrows that pool and runs again.
+// output sizes) stay on the device.  The data-dependent bounds -- the
+// (y, f tile) key space and the probe bound of the sketch-sized tables --
+// are checked on the device; on overflow the host regrows that pool (or
+// falls back to tuple-sized tables) and runs again.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
